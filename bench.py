@@ -1,0 +1,375 @@
+"""Throughput benchmark: D3Q19 channel 256x128x128 (inflow u_x = 0.04, pressure outflow rho = 1,
+no-slip walls, solid sphere r = 16 at (64, 64, 64), omega = 1.8), populations stored as FP32
+(the headline) and FP16 (shifted by w_q), one fused step kernel per time step.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line. `value` is MLUPS over interior cells (xl*yl*zl*K / seconds) with the state
+resident in HBM, timed with CUDA events on the library's stream; `e2e` is the same metric through
+the C ABI with the initial state uploaded from pinned host memory and a per-step FP64 mass and
+momentum read-back inside the timed region. With --impl reference the CPU solver of the reference
+(the C restatement under oracle/, or the reference's own build where it exists) is timed on the
+host cores on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "D3Q19 MLUPS & % HBM roofline, FP16-store vs FP32 at stated FP64 error"
+WORKLOAD = "channel 256x128x128, sphere r16 at (64,64,64), u_in 0.04, omega 1.8"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=400)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--size", default="256,128,128")
+    ap.add_argument("--quick", action="store_true", help="headline only (no stencil sweep / e2e / cpu)")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def workload(q: int, size):
+    from lbm_gb300 import scenario as S
+    xl, yl, zl = size
+    return S.channel(xl, yl, zl, q=q, u_in=0.04, omega=1.8,
+                     sphere=((xl // 4, yl // 2, zl // 2), max(1, yl // 8)))
+
+
+def measured_peak():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel_tag: str):
+    """DRAM bytes per launch of the step kernel from the committed ncu summary, or None."""
+    f = ROOT / "profiles" / "traffic.txt"
+    if not f.exists():
+        return None
+    for line in f.read_text().splitlines():
+        parts = line.split()
+        if len(parts) >= 2 and parts[0] == kernel_tag:
+            return float(parts[1])
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons, sampled every 200 ms while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def time_steps(dom, steps: int, warmup: int):
+    """Warm up, then time `steps` single-step launches with CUDA events on the library's stream.
+    Returns seconds."""
+    import torch
+    dom.step(warmup)
+    dom.sync()
+    stream = torch.cuda.ExternalStream(dom.stream_handle())
+    start = torch.cuda.Event(enable_timing=True)
+    end = torch.cuda.Event(enable_timing=True)
+    start.record(stream)
+    for _ in range(steps):
+        dom.step(1)
+    end.record(stream)
+    end.synchronize()
+    return start.elapsed_time(end) / 1e3
+
+
+def run_ours(args, rank, world, local):
+    import torch
+    import torch.distributed as dist
+
+    from lbm_gb300 import build_domain, capi
+    torch.cuda.set_device(local)
+    size = tuple(int(v) for v in args.size.split(","))
+    K, W = args.steps, args.warmup
+    peak, peak_kind = measured_peak()
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def max_over_ranks(x: float) -> float:
+        if world == 1:
+            return x
+        t = torch.tensor([x], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    results = {}
+    scn19 = workload(19, size)
+    ncell = scn19.ninterior
+
+    # headline: D3Q19 FP32, clocks sampled during the timed region
+    dom = build_domain(scn19, "fp32")
+    info = dom.memory_info()
+    barrier()
+    with ClockSampler(local) as clk:
+        sec = time_steps(dom, K, W)
+    barrier()
+    sec = max_over_ranks(sec)
+    results["fp32"] = (sec, info)
+    clocks = clk.summary()
+    u32 = dom.moments()[1]
+    dom.close()
+
+    # FP16 storage, same workload
+    dom = build_domain(scn19, "fp16")
+    info16 = dom.memory_info()
+    barrier()
+    sec16 = max_over_ranks(time_steps(dom, K, W))
+    u16 = dom.moments()[1]
+    dom.close()
+
+    out_extra = {}
+    if not args.quick:
+        # FP64 run of the same W + K steps: the error statement for the reduced precisions
+        dom = build_domain(scn19, "fp64")
+        dom.step(W + K)
+        u64 = dom.moments()[1]
+        dom.close()
+        fl = scn19.fluid_mask_interior()
+
+        def err(u):
+            return float(np.linalg.norm(u[fl] - u64[fl]) / np.linalg.norm(u64[fl]))
+        out_extra["u_rel_l2_vs_fp64"] = {"fp32": err(u32), "fp16": err(u16), "steps": W + K}
+        # other stencils, FP32
+        sten = {}
+        for q in (15, 27):
+            d = build_domain(workload(q, size), "fp32")
+            s = max_over_ranks(time_steps(d, K, W))
+            mi = d.memory_info()
+            sten[f"D3Q{q}"] = {"mlups": world * ncell * K / s / 1e6,
+                               "hbm_frac": mi["step_bytes"] * K / s / 1e9 / peak}
+            d.close()
+        out_extra["stencils_fp32"] = sten
+
+    ms = sec / K * 1e3
+    mlups = world * ncell * K / sec / 1e6
+    achieved = info["step_bytes"] / (sec / K) / 1e9
+    traffic = ncu_traffic("step_kernel_d3q19_fp32")
+    line = {
+        "metric": METRIC, "value": mlups, "unit": "MLUPS", "n_gpus": world, "steps": K, "warmup": W,
+        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "lattice": "D3Q19", "size": list(size), "storage": "fp32 (f - w)",
+                   "cells": ncell, "fluid_cells": info["fluid_cells"], "parallelism": f"replicas x{world}",
+                   "l2": "inputs larger than L2 (%.0f MB populations per step > 129 MB)" % (info["step_bytes"] / 2e6)},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": peak_kind, "traffic": traffic,
+                     "algorithmic_bytes_per_launch": info["step_bytes"]},
+        "fp16": {"value": world * ncell * K / sec16 / 1e6, "ms_per_step": sec16 / K * 1e3,
+                 "achieved_gbs": info16["step_bytes"] / (sec16 / K) / 1e9,
+                 "frac": info16["step_bytes"] / (sec16 / K) / 1e9 / peak,
+                 "speedup_vs_fp32": sec / sec16},
+        "gpu_launches": K,
+        "clocks": clocks,
+    }
+    line.update(out_extra)
+    if not args.quick:
+        line["e2e"] = run_e2e(scn19, K, W)
+        if rank == 0:
+            line["cpu_baseline"] = cpu_baseline(size, budget_s=12.0)
+    return line if rank == 0 else None
+
+
+def run_e2e(scn, K, W):
+    """Same metric through the C ABI with host buffers: upload the initial state from pinned host
+    memory, K x (lbm_step + FP64 mass/momentum read-back), final moments read-back."""
+    import torch
+
+    from lbm_gb300 import build_domain
+    dom = build_domain(scn, "fp32")
+    f0 = torch.empty((scn.ncells, scn.q), dtype=torch.float64).pin_memory()
+    f0.numpy()[:] = np.tile(scn.model.weights, (scn.ncells, 1))
+    lib = dom._lib
+    out = np.empty(4)
+    rho = np.empty(scn.ninterior)
+    u = np.empty(3 * scn.ninterior)
+    dom.step(W)
+    dom.sync()
+    t0 = time.perf_counter()
+    rc = lib.lbm_set_populations(dom._h, ctypes.c_void_p(f0.data_ptr()))
+    for _ in range(K):
+        rc |= lib.lbm_step(dom._h, 1)
+        rc |= lib.lbm_reduce_mass_momentum(dom._h, out.ctypes.data)
+    rc |= lib.lbm_moments(dom._h, rho.ctypes.data, u.ctypes.data)
+    t1 = time.perf_counter()
+    dom.close()
+    if rc:
+        raise RuntimeError("e2e run failed")
+    h2d = scn.ncells * scn.q * 8
+    d2h = 32 * K + 32 * scn.ninterior
+    return {"value": scn.ninterior * K / (t1 - t0) / 1e6, "unit": "MLUPS", "h2d_bytes_per_step": h2d / K,
+            "d2h_bytes_per_step": d2h / K, "seconds": t1 - t0}
+
+
+def cpu_threads() -> int:
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def cpu_run(size, steps: int, threads: int, kind: str):
+    import oracle
+    scn = workload(19, size)
+    if kind == "reference":
+        r = oracle.run_ref(scn, steps, threads=threads, fast=True, want_pops=False)
+        return r["seconds"]
+    c = oracle.Checker(scn)
+    sec = c.step(steps, threads)
+    c.close()
+    return sec
+
+
+def cpu_kind() -> str:
+    import oracle
+    return "reference" if oracle.checkers.REF_LIB_FAST.exists() else "port"
+
+
+def cpu_baseline(size, budget_s: float):
+    """The reference CPU solver on all host cores, on a bounded number of steps of the same
+    workload (about `budget_s` seconds)."""
+    import oracle
+    oracle.build(with_ref=False) if not oracle.port_available() else None
+    threads = cpu_threads()
+    kind = cpu_kind()
+    probe = cpu_run(size, 2, threads, kind) / 2
+    steps = int(max(2, min(200, budget_s / max(probe, 1e-6))))
+    sec = cpu_run(size, steps, threads, kind)
+    ncell = size[0] * size[1] * size[2]
+    return {"value": ncell * steps / sec / 1e6, "unit": "MLUPS", "cores": threads, "kind": kind,
+            "sample": f"{steps} steps of the full {size[0]}x{size[1]}x{size[2]} D3Q19 channel (FP64, "
+                      f"reference algorithm: AoS pull-stream + two-phase collide, OpenMP)"}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return None
+    size = tuple(int(v) for v in args.size.split(","))
+    import oracle
+    if not oracle.port_available():
+        oracle.build(with_ref=False)
+    threads = cpu_threads()
+    kind = cpu_kind()
+    ncell = size[0] * size[1] * size[2]
+    probe = cpu_run(size, 1, threads, kind)
+    K, W = args.steps, args.warmup
+    # bound the run to about two minutes: each timed step is one full step of the workload
+    k_run = int(max(1, min(K, 100.0 / max(probe, 1e-6))))
+    w_run = int(max(0, min(W, 20.0 / max(probe, 1e-6))))
+    if w_run:
+        cpu_run(size, w_run, threads, kind)
+    sec = cpu_run(size, k_run, threads, kind)
+    mlups = ncell * k_run / sec / 1e6
+    sample = (f"{k_run} timed steps (of {K} requested) after {w_run} warm-up steps of the full "
+              f"{size[0]}x{size[1]}x{size[2]} D3Q19 channel, FP64")
+    return {
+        "impl": "reference", "metric": METRIC, "value": mlups, "unit": "MLUPS", "n_gpus": world, "steps": K,
+        "warmup": W, "ms_per_step": sec / k_run * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "lattice": "D3Q19", "size": list(size), "storage": "fp64 AoS, two fields"},
+        "cpu_baseline": {"value": mlups, "unit": "MLUPS", "cores": threads, "kind": kind, "sample": sample},
+        "e2e": {"value": mlups, "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        line = run_reference(args, rank, world)
+        if line is not None:
+            print(json.dumps(line), flush=True)
+        return
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    line = run_ours(args, rank, world, local)
+    if line is not None:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,81 @@
+"""Compile the CUDA step library (lbm_gb300/_lib/liblbm_gb300.so) for sm_103a with nvcc.
+
+Translation units compile in parallel; a unit is rebuilt only when one of the sources is newer
+than its object file. The FP64 unit is compiled with -fmad=false so that no multiply-add is
+fused there (the FP64 path reproduces the reference's rounding exactly).
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+from concurrent.futures import ThreadPoolExecutor
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+CSRC = PKG / "csrc"
+LIBDIR = PKG / "_lib"
+OBJDIR = LIBDIR / "obj"
+LIB = LIBDIR / "liblbm_gb300.so"
+INCLUDE = PKG.parent / "include"
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+COMMON = ["-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
+          "-Xcompiler", "-O2"]
+UNITS = {
+    "capi": [],
+    "step_fp64": ["-fmad=false"],
+    "step_fp32": [],
+    "step_fp16": [],
+    "step_bf16": [],
+}
+
+
+def nvcc() -> str:
+    path = shutil.which("nvcc")
+    if path:
+        return path
+    cand = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda")) / "bin" / "nvcc"
+    if cand.exists():
+        return str(cand)
+    raise RuntimeError("nvcc not found: the CUDA toolkit is required to build liblbm_gb300.so")
+
+
+def _deps() -> list[Path]:
+    return sorted(CSRC.glob("*.cuh")) + [INCLUDE / "lbm_gb300.h"]
+
+
+def _compile(name: str, extra: list[str], verbose: bool) -> Path:
+    src = CSRC / f"{name}.cu"
+    obj = OBJDIR / f"{name}.o"
+    newest = max(p.stat().st_mtime for p in _deps() + [src])
+    if obj.exists() and obj.stat().st_mtime >= newest:
+        return obj
+    cmd = [nvcc(), *ARCH, *COMMON, *extra, "-c", str(src), "-o", str(obj)]
+    if verbose:
+        cmd.insert(1, "-Xptxas=-v")
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"nvcc failed for {src.name}:\n{res.stdout}\n{res.stderr}")
+    if verbose and res.stderr:
+        print(res.stderr)
+    return obj
+
+
+def build(verbose: bool = False) -> Path:
+    """Compile every translation unit (in parallel) and link liblbm_gb300.so; returns its path."""
+    OBJDIR.mkdir(parents=True, exist_ok=True)
+    with ThreadPoolExecutor(max_workers=len(UNITS)) as pool:
+        objs = list(pool.map(lambda kv: _compile(kv[0], kv[1], verbose), UNITS.items()))
+    if not LIB.exists() or LIB.stat().st_mtime < max(o.stat().st_mtime for o in objs):
+        cmd = [nvcc(), *ARCH, "-shared", "-o", str(LIB), *map(str, objs)]
+        res = subprocess.run(cmd, capture_output=True, text=True)
+        if res.returncode != 0:
+            raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")
+    return LIB
+
+
+if __name__ == "__main__":
+    import sys
+
+    print(build(verbose="-v" in sys.argv))

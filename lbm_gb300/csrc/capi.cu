@@ -1,0 +1,644 @@
+// Host side of the C ABI declared in include/lbm_gb300.h.
+//
+// A handle keeps the geometry as a host byte map in the device layout (one byte per cell:
+// fluid, ghost-fluid or handler id), the handler table, and the device state. Geometry calls
+// only touch the host map; the next call that needs the device state uploads it, classifies the
+// fluid cells, rebuilds the side-pass lists and, when the populations are no longer the initial
+// ones, carries them across the change (read back with the old geometry, written with the new).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/lbm_gb300.h"
+#include "domain.cuh"
+#include "lattice.cuh"
+#include "ops.cuh"
+
+using namespace lbmg;
+
+namespace {
+
+thread_local std::string g_create_error;
+
+struct CudaError : std::runtime_error {
+    int code;
+    CudaError(const std::string& what, int c) : std::runtime_error(what), code(c) {}
+};
+struct ArgError : std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
+struct StateError : std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
+
+void check(cudaError_t e, const char* what)
+{
+    if (e != cudaSuccess) {
+        const int code = (e == cudaErrorMemoryAllocation) ? LBM_ERR_OOM : LBM_ERR_CUDA;
+        throw CudaError(std::string(what) + ": " + cudaGetErrorString(e), code);
+    }
+}
+
+size_t store_bytes(int precision) { return precision == LBM_FP64 ? 8 : (precision == LBM_FP32 ? 4 : 2); }
+
+// Lattice velocity component, host side.
+int lat_c(int q, int Q, int d)
+{
+    switch (Q) {
+    case 15: return Lattice<15>::c(q, d);
+    case 19: return Lattice<19>::c(q, d);
+    default: return Lattice<27>::c(q, d);
+    }
+}
+double lat_w(int q, int Q)
+{
+    switch (Q) {
+    case 15: return Lattice<15>::w(q);
+    case 19: return Lattice<19>::w(q);
+    default: return Lattice<27>::w(q);
+    }
+}
+int lat_velocity_index(int Q, int u, int v, int w)
+{
+    switch (Q) {
+    case 15: return Lattice<15>::velocity_index(u, v, w);
+    case 19: return Lattice<19>::velocity_index(u, v, w);
+    default: return Lattice<27>::velocity_index(u, v, w);
+    }
+}
+
+template <class T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf() { release(); }
+    void alloc(size_t count, const char* what)
+    {
+        release();
+        if (count == 0) return;
+        check(cudaMalloc(reinterpret_cast<void**>(&p), count * sizeof(T)), what);
+        n = count;
+    }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    size_t bytes() const { return n * sizeof(T); }
+};
+
+}  // namespace
+
+struct lbm_domain {
+    DomainDev dev{};
+    const KernelOps* ops = nullptr;
+    cudaStream_t stream = nullptr;
+    int Q = 0;
+    int precision = 0;
+    size_t ng = 0;         // cells incl. ghost layer
+    size_t n_interior = 0;
+    uint64_t fluid_cells = 0;
+
+    std::vector<uint8_t> hmap;                  // PS bytes, device layout
+    std::vector<BcEntry> bcs;                   // handler h at index h-1
+    std::vector<std::vector<double>> profiles;  // per handler: empty or 3*ng doubles
+
+    bool geom_dirty = true;
+    bool state_custom = false;
+    long long steps = 0;
+
+    DevBuf<unsigned char> pop;
+    DevBuf<uint8_t> flag;
+    DevBuf<BcEntry> bc;
+    DevBuf<double> profile;
+    DevBuf<int> gf_xyz;
+    DevBuf<double> gf_pop;
+    DevBuf<int4> fs_link;
+    DevBuf<double> red;  // 4 * kReduceBlocks partials + 4 totals
+
+    std::string err;
+
+    ~lbm_domain()
+    {
+        pop.release(); flag.release(); bc.release(); profile.release();
+        gf_xyz.release(); gf_pop.release(); fs_link.release(); red.release();
+        if (stream) cudaStreamDestroy(stream);
+    }
+
+    size_t layout_index(int x, int y, int z) const
+    {
+        return static_cast<size_t>(kXOff + x) +
+               static_cast<size_t>(dev.g.XS) *
+                   (static_cast<size_t>(y) + static_cast<size_t>(dev.g.YS) * static_cast<size_t>(z));
+    }
+    size_t ref_index(int x, int y, int z) const
+    {
+        return static_cast<size_t>(x) +
+               static_cast<size_t>(dev.g.xl + 2) *
+                   (static_cast<size_t>(y) + static_cast<size_t>(dev.g.yl + 2) * static_cast<size_t>(z));
+    }
+    bool interior(int x, int y, int z) const
+    {
+        return x >= 1 && x <= dev.g.xl && y >= 1 && y <= dev.g.yl && z >= 1 && z <= dev.g.zl;
+    }
+    bool on_periodic_ghost(int x, int y, int z) const
+    {
+        const Geom& g = dev.g;
+        return ((g.per & 1) && (x == 0 || x == g.xl + 1)) || ((g.per & 2) && (y == 0 || y == g.yl + 1)) ||
+               ((g.per & 4) && (z == 0 || z == g.zl + 1));
+    }
+    void wrap(int& x, int& y, int& z) const
+    {
+        const Geom& g = dev.g;
+        auto w = [](int v, int l, bool p) { return p ? (v < 1 ? v + l : (v > l ? v - l : v)) : v; };
+        x = w(x, g.xl, g.per & 1);
+        y = w(y, g.yl, g.per & 2);
+        z = w(z, g.zl, g.per & 4);
+    }
+    uint8_t hm(int x, int y, int z) const { return hmap[layout_index(x, y, z)]; }
+
+    void finalize();
+    void build_side_lists();
+};
+
+// Ghost-fluid cells adjacent to interior fluid (or used as a free-slip source) and the
+// free-slip links, from the host map.
+void lbm_domain::build_side_lists()
+{
+    const Geom& g = dev.g;
+    // earlier work on the stream may still read the lists released below
+    check(cudaStreamSynchronize(stream), "side-list rebuild");
+    std::vector<int> gxyz;
+    auto gf_lookup = [&](int x, int y, int z) -> int {
+        for (size_t j = 0; j < gxyz.size() / 3; ++j)
+            if (gxyz[3 * j] == x && gxyz[3 * j + 1] == y && gxyz[3 * j + 2] == z) return static_cast<int>(j);
+        gxyz.push_back(x); gxyz.push_back(y); gxyz.push_back(z);
+        return static_cast<int>(gxyz.size() / 3 - 1);
+    };
+    auto is_fluid_h = [&](int x, int y, int z) {
+        const uint8_t v = hm(x, y, z);
+        return v < kFirstHandler && !on_periodic_ghost(x, y, z);  // interior fluid or ghost fluid
+    };
+    auto interior_fluid_h = [&](int x, int y, int z) { return interior(x, y, z) && hm(x, y, z) == 0; };
+
+    // ghost-fluid cells with an interior fluid neighbour
+    for (int z = 0; z <= g.zl + 1; ++z)
+        for (int y = 0; y <= g.yl + 1; ++y)
+            for (int x = 0; x <= g.xl + 1; ++x) {
+                if (interior(x, y, z) || on_periodic_ghost(x, y, z)) continue;
+                if (hm(x, y, z) != kGhostFluid) continue;
+                bool adj = false;
+                for (int q = 0; q < Q && !adj; ++q) {
+                    int nx = x + lat_c(q, Q, 0), ny = y + lat_c(q, Q, 1), nz = z + lat_c(q, Q, 2);
+                    wrap(nx, ny, nz);
+                    if (interior_fluid_h(nx, ny, nz)) adj = true;
+                }
+                if (adj) { gxyz.push_back(x); gxyz.push_back(y); gxyz.push_back(z); }
+            }
+
+    // free-slip links (boundary.hpp:79-115)
+    std::vector<int4> links;
+    for (int z = 0; z <= g.zl + 1; ++z)
+        for (int y = 0; y <= g.yl + 1; ++y)
+            for (int x = 0; x <= g.xl + 1; ++x) {
+                const uint8_t v = hm(x, y, z);
+                if (v < kFirstHandler || on_periodic_ghost(x, y, z)) continue;
+                if (bcs[v - kFirstHandler].type != kFreeSlip) continue;
+                for (int q = 0; q < Q; ++q) {
+                    const int dx = lat_c(q, Q, 0), dy = lat_c(q, Q, 1), dz = lat_c(q, Q, 2);
+                    int nx = x + dx, ny = y + dy, nz = z + dz;
+                    wrap(nx, ny, nz);
+                    if (!interior_fluid_h(nx, ny, nz)) continue;
+                    const int cand[6][3] = {{x + dx, y, z}, {x, y + dy, z}, {x, y, z + dz},
+                                            {x, y + dy, z + dz}, {x + dx, y, z + dz}, {x + dx, y + dy, z}};
+                    const int mir[6][3] = {{-dx, dy, dz}, {dx, -dy, dz}, {dx, dy, -dz},
+                                           {dx, -dy, -dz}, {-dx, dy, -dz}, {-dx, -dy, dz}};
+                    for (int k = 0; k < 6; ++k) {
+                        int sx = cand[k][0], sy = cand[k][1], sz = cand[k][2];
+                        wrap(sx, sy, sz);
+                        if (!is_fluid_h(sx, sy, sz)) continue;
+                        const int qs = lat_velocity_index(Q, mir[k][0], mir[k][1], mir[k][2]);
+                        if (qs < 0 || qs >= Q) break;
+                        int4 l;
+                        l.x = static_cast<int>(layout_index(nx, ny, nz));
+                        if (interior(sx, sy, sz)) {
+                            int mx = sx + lat_c(qs, Q, 0), my = sy + lat_c(qs, Q, 1), mz = sz + lat_c(qs, Q, 2);
+                            wrap(mx, my, mz);
+                            l.y = q | (qs << 8);
+                            l.z = static_cast<int>(layout_index(sx, sy, sz));
+                            l.w = static_cast<int>(layout_index(mx, my, mz));
+                        } else {
+                            l.y = q | (qs << 8) | (1 << 16);
+                            l.z = gf_lookup(sx, sy, sz);
+                            l.w = 0;
+                        }
+                        links.push_back(l);
+                        break;
+                    }
+                }
+            }
+
+    gf_xyz.release(); gf_pop.release(); fs_link.release();
+    dev.n_gf = static_cast<int>(gxyz.size() / 3);
+    dev.n_fs = static_cast<int>(links.size());
+    if (dev.n_gf > 0) {
+        gf_xyz.alloc(gxyz.size(), "cudaMalloc(ghost-fluid list)");
+        check(cudaMemcpyAsync(gf_xyz.p, gxyz.data(), gxyz.size() * sizeof(int), cudaMemcpyHostToDevice, stream),
+              "upload ghost-fluid list");
+        gf_pop.alloc(static_cast<size_t>(2) * dev.n_gf * Q, "cudaMalloc(ghost-fluid populations)");
+        std::vector<double> w(static_cast<size_t>(2) * dev.n_gf * Q);
+        for (size_t k = 0; k < w.size(); ++k) w[k] = lat_w(static_cast<int>(k % Q), Q);
+        check(cudaMemcpyAsync(gf_pop.p, w.data(), w.size() * sizeof(double), cudaMemcpyHostToDevice, stream),
+              "init ghost-fluid populations");
+        check(cudaStreamSynchronize(stream), "ghost-fluid setup");
+    }
+    if (dev.n_fs > 0) {
+        fs_link.alloc(links.size(), "cudaMalloc(free-slip links)");
+        check(cudaMemcpyAsync(fs_link.p, links.data(), links.size() * sizeof(int4), cudaMemcpyHostToDevice, stream),
+              "upload free-slip links");
+        check(cudaStreamSynchronize(stream), "free-slip setup");
+    }
+    dev.gf_xyz = gf_xyz.p;
+    dev.gf_pop = gf_pop.p;
+    dev.fs_link = fs_link.p;
+}
+
+void lbm_domain::finalize()
+{
+    if (!geom_dirty) return;
+    const Geom& g = dev.g;
+    DevBuf<double> carry;
+    if (state_custom) {
+        // the current state, read with the geometry it was produced under
+        carry.alloc(ng * Q, "cudaMalloc(state carry-over)");
+        ops->gather(dev, steps, carry.p, stream);
+    }
+    check(cudaMemcpyAsync(flag.p, hmap.data(), hmap.size(), cudaMemcpyHostToDevice, stream), "upload flags");
+    ops->classify(dev, stream);
+    check(cudaMemcpyAsync(bc.p, bcs.data(), bcs.size() * sizeof(BcEntry), cudaMemcpyHostToDevice, stream),
+          "upload handler table");
+    // merged inflow profile in reference cell order
+    bool any_profile = false;
+    for (const auto& p : profiles) any_profile = any_profile || !p.empty();
+    if (any_profile) {
+        std::vector<double> merged(3 * ng, 0.0);
+        for (int z = 0; z <= g.zl + 1; ++z)
+            for (int y = 0; y <= g.yl + 1; ++y)
+                for (int x = 0; x <= g.xl + 1; ++x) {
+                    const uint8_t v = hm(x, y, z);
+                    if (v < kFirstHandler) continue;
+                    const auto& p = profiles[v - kFirstHandler];
+                    if (p.empty()) continue;
+                    const size_t r = ref_index(x, y, z);
+                    merged[3 * r] = p[3 * r]; merged[3 * r + 1] = p[3 * r + 1]; merged[3 * r + 2] = p[3 * r + 2];
+                }
+        if (!profile.p) profile.alloc(3 * ng, "cudaMalloc(inflow profile)");
+        check(cudaMemcpyAsync(profile.p, merged.data(), merged.size() * sizeof(double), cudaMemcpyHostToDevice, stream),
+              "upload inflow profile");
+        check(cudaStreamSynchronize(stream), "inflow profile");
+    }
+    dev.profile = profile.p;
+    build_side_lists();
+    fluid_cells = 0;
+    for (int z = 1; z <= g.zl; ++z)
+        for (int y = 1; y <= g.yl; ++y) {
+            const uint8_t* row = hmap.data() + layout_index(1, y, z);
+            for (int x = 0; x < g.xl; ++x) fluid_cells += row[x] == 0;
+        }
+    if (state_custom) {
+        ops->scatter(dev, steps, carry.p, stream);
+        check(cudaStreamSynchronize(stream), "state carry-over");
+        carry.release();
+    }
+    check(cudaGetLastError(), "finalize kernels");
+    geom_dirty = false;
+}
+
+namespace {
+
+template <class F>
+int guarded(lbm_domain* d, F&& f)
+{
+    if (!d) return LBM_ERR_ARG;
+    try {
+        f();
+        return LBM_OK;
+    } catch (const CudaError& e) {
+        d->err = e.what();
+        return e.code;
+    } catch (const ArgError& e) {
+        d->err = e.what();
+        return LBM_ERR_ARG;
+    } catch (const StateError& e) {
+        d->err = e.what();
+        return LBM_ERR_STATE;
+    } catch (const std::bad_alloc&) {
+        d->err = "host allocation failed";
+        return LBM_ERR_OOM;
+    } catch (const std::exception& e) {
+        d->err = e.what();
+        return LBM_ERR_CUDA;
+    } catch (...) {
+        d->err = "unknown error";
+        return LBM_ERR_CUDA;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int lbm_create(lbm_domain** out, int q, int64_t xl, int64_t yl, int64_t zl, double tau, int precision)
+{
+    g_create_error.clear();
+    if (!out) { g_create_error = "out is NULL"; return LBM_ERR_ARG; }
+    *out = nullptr;
+    if (q != 15 && q != 19 && q != 27) { g_create_error = "lattice model must be 15, 19 or 27"; return LBM_ERR_ARG; }
+    if (!(tau > 0.5 && tau < 2.0)) { g_create_error = "tau must lie in (0.5, 2.0)"; return LBM_ERR_ARG; }
+    if (xl < 1 || yl < 1 || zl < 1) { g_create_error = "domain lengths must be positive"; return LBM_ERR_ARG; }
+    if (precision < LBM_FP64 || precision > LBM_BF16) { g_create_error = "unknown precision"; return LBM_ERR_ARG; }
+    const int64_t XS = (xl + 2 + 31) / 32 * 32, YS = yl + 2, ZS = zl + 2;
+    const int64_t cells = XS * YS * ZS;
+    if (xl > (1 << 20) || yl > 65535 || zl > 65535 || cells + 64 >= (int64_t(1) << 31)) {
+        g_create_error = "domain too large (cell index must fit 31 bits, yl and zl <= 65535)";
+        return LBM_ERR_ARG;
+    }
+    lbm_domain* d = nullptr;
+    try {
+        d = new lbm_domain();
+    } catch (...) {
+        g_create_error = "host allocation failed";
+        return LBM_ERR_OOM;
+    }
+    const int rc = guarded(d, [&] {
+        d->Q = q;
+        d->precision = precision;
+        Geom& g = d->dev.g;
+        g.xl = static_cast<int>(xl); g.yl = static_cast<int>(yl); g.zl = static_cast<int>(zl);
+        g.XS = static_cast<int>(XS); g.YS = static_cast<int>(YS); g.ZS = static_cast<int>(ZS);
+        g.per = 0;
+        g.PS = static_cast<size_t>((cells + 32 + 63) / 64 * 64);
+        d->ng = static_cast<size_t>(xl + 2) * (yl + 2) * (zl + 2);
+        d->n_interior = static_cast<size_t>(xl) * yl * zl;
+        d->dev.q = q;
+        d->dev.precision = precision;
+        d->dev.tau = tau;
+        switch (precision) {
+        case LBM_FP64: d->ops = ops_fp64(q); break;
+        case LBM_FP32: d->ops = ops_fp32(q); break;
+        case LBM_FP16: d->ops = ops_fp16(q); break;
+        default: d->ops = ops_bf16(q); break;
+        }
+        check(cudaStreamCreateWithFlags(&d->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+        d->pop.alloc(static_cast<size_t>(q) * g.PS * store_bytes(precision), "cudaMalloc(populations)");
+        d->flag.alloc(g.PS, "cudaMalloc(flags)");
+        d->bc.alloc(kMaxHandlers, "cudaMalloc(handler table)");
+        d->red.alloc(4 * kReduceBlocks + 4, "cudaMalloc(reduction scratch)");
+        d->dev.pop = d->pop.p;
+        d->dev.flag = d->flag.p;
+        d->dev.bc = d->bc.p;
+        // host map: interior cells fluid, everything else ghost-fluid until a handler is set
+        d->hmap.assign(g.PS, kGhostFluid);
+        for (int z = 1; z <= g.zl; ++z)
+            for (int y = 1; y <= g.yl; ++y)
+                std::memset(d->hmap.data() + d->layout_index(1, y, z), 0, static_cast<size_t>(g.xl));
+        d->ops->init(d->dev, d->stream);
+        check(cudaGetLastError(), "init kernel");
+        check(cudaStreamSynchronize(d->stream), "init");
+    });
+    if (rc != LBM_OK) {
+        g_create_error = d->err;
+        delete d;
+        return rc;
+    }
+    *out = d;
+    return LBM_OK;
+}
+
+void lbm_destroy(lbm_domain* d)
+{
+    if (!d) return;
+    if (d->stream) cudaStreamSynchronize(d->stream);
+    delete d;
+}
+
+int lbm_add_boundary(lbm_domain* d, int type, const double params[4], int* handler)
+{
+    return guarded(d, [&] {
+        if (type < LBM_NOSLIP || type > LBM_PRESSURE) throw ArgError("unknown boundary type");
+        if (static_cast<int>(d->bcs.size()) >= kMaxHandlers) throw ArgError("too many boundary handlers");
+        BcEntry b{};
+        b.type = type;
+        b.has_profile = 0;
+        if (params) {
+            for (int k = 0; k < 4; ++k)
+                if (!std::isfinite(params[k])) throw ArgError("boundary parameters must be finite");
+            b.v[0] = params[0]; b.v[1] = params[1]; b.v[2] = params[2];
+            b.rho = params[3];
+        } else {
+            b.rho = 1.0;
+        }
+        if ((type == LBM_OUTFLOW || type == LBM_PRESSURE) && b.rho == 0.0)
+            throw ArgError("reference density must be nonzero");
+        d->bcs.push_back(b);
+        d->profiles.emplace_back();
+        d->geom_dirty = true;
+        if (handler) *handler = static_cast<int>(d->bcs.size());
+    });
+}
+
+int lbm_set_boundary_box(lbm_domain* d, int handler, const int64_t box[6])
+{
+    return guarded(d, [&] {
+        if (handler < 1 || handler > static_cast<int>(d->bcs.size())) throw ArgError("unknown handler");
+        if (!box) throw ArgError("box is NULL");
+        const Geom& g = d->dev.g;
+        // domain.hpp:180-181
+        if (!(box[1] >= box[0] && box[3] >= box[2] && box[5] >= box[4])) throw ArgError("box end before begin");
+        if (box[0] < 0 || box[2] < 0 || box[4] < 0 || box[1] >= g.xl + 2 || box[3] >= g.yl + 2 || box[5] >= g.zl + 2)
+            throw ArgError("box outside the domain (ghost layer included)");
+        const uint8_t v = static_cast<uint8_t>(kFirstHandler + handler - 1);
+        for (int64_t z = box[4]; z <= box[5]; ++z)
+            for (int64_t y = box[2]; y <= box[3]; ++y)
+                std::memset(d->hmap.data() + d->layout_index(static_cast<int>(box[0]), static_cast<int>(y), static_cast<int>(z)),
+                            v, static_cast<size_t>(box[1] - box[0] + 1));
+        d->geom_dirty = true;
+    });
+}
+
+int lbm_set_solid_mask(lbm_domain* d, const uint8_t* mask, int* handler)
+{
+    return guarded(d, [&] {
+        if (!mask) throw ArgError("mask is NULL");
+        if (static_cast<int>(d->bcs.size()) >= kMaxHandlers) throw ArgError("too many boundary handlers");
+        BcEntry b{};
+        b.type = kNoSlip;
+        b.rho = 1.0;
+        d->bcs.push_back(b);
+        d->profiles.emplace_back();
+        const int h = static_cast<int>(d->bcs.size());
+        const uint8_t v = static_cast<uint8_t>(kFirstHandler + h - 1);
+        const Geom& g = d->dev.g;
+        size_t m = 0;
+        for (int z = 1; z <= g.zl; ++z)
+            for (int y = 1; y <= g.yl; ++y) {
+                uint8_t* row = d->hmap.data() + d->layout_index(1, y, z);
+                for (int x = 0; x < g.xl; ++x, ++m)
+                    if (mask[m]) row[x] = v;
+            }
+        d->geom_dirty = true;
+        if (handler) *handler = h;
+    });
+}
+
+int lbm_set_periodic(lbm_domain* d, int px, int py, int pz)
+{
+    return guarded(d, [&] {
+        d->dev.g.per = (px ? 1 : 0) | (py ? 2 : 0) | (pz ? 4 : 0);
+        d->geom_dirty = true;
+    });
+}
+
+int lbm_set_inflow_profile(lbm_domain* d, int handler, const double* u_cells)
+{
+    return guarded(d, [&] {
+        if (handler < 1 || handler > static_cast<int>(d->bcs.size())) throw ArgError("unknown handler");
+        if (d->bcs[handler - 1].type != kInflow) throw ArgError("handler is not an inflow boundary");
+        if (!u_cells) throw ArgError("u_cells is NULL");
+        d->profiles[handler - 1].assign(u_cells, u_cells + 3 * d->ng);
+        d->bcs[handler - 1].has_profile = 1;
+        d->geom_dirty = true;
+    });
+}
+
+int lbm_set_nonfluid_cells_nullcollide(lbm_domain* d)
+{
+    return guarded(d, [&] {});
+}
+
+int lbm_set_populations(lbm_domain* d, const double* f)
+{
+    return guarded(d, [&] {
+        if (!f) throw ArgError("f is NULL");
+        d->finalize();
+        DevBuf<double> tmp;
+        tmp.alloc(d->ng * d->Q, "cudaMalloc(population staging)");
+        check(cudaMemcpyAsync(tmp.p, f, tmp.bytes(), cudaMemcpyHostToDevice, d->stream), "upload populations");
+        d->ops->scatter(d->dev, d->steps, tmp.p, d->stream);
+        check(cudaGetLastError(), "scatter kernel");
+        check(cudaStreamSynchronize(d->stream), "set populations");
+        d->state_custom = true;
+    });
+}
+
+int lbm_get_populations(lbm_domain* d, double* f)
+{
+    return guarded(d, [&] {
+        if (!f) throw ArgError("f is NULL");
+        d->finalize();
+        DevBuf<double> tmp;
+        tmp.alloc(d->ng * d->Q, "cudaMalloc(population staging)");
+        d->ops->gather(d->dev, d->steps, tmp.p, d->stream);
+        check(cudaGetLastError(), "gather kernel");
+        check(cudaMemcpyAsync(f, tmp.p, tmp.bytes(), cudaMemcpyDeviceToHost, d->stream), "download populations");
+        check(cudaStreamSynchronize(d->stream), "get populations");
+    });
+}
+
+int lbm_step(lbm_domain* d, int64_t nsteps)
+{
+    return guarded(d, [&] {
+        if (nsteps < 0) throw ArgError("nsteps must be >= 0");
+        d->finalize();
+        for (int64_t k = 0; k < nsteps; ++k) d->ops->step(d->dev, d->steps + 1 + k, d->stream);
+        check(cudaGetLastError(), "step kernel launch");
+        d->steps += nsteps;
+        if (nsteps > 0) d->state_custom = true;
+    });
+}
+
+int lbm_moments(lbm_domain* d, double* rho, double* u)
+{
+    return guarded(d, [&] {
+        if (!rho) throw ArgError("rho is NULL");
+        d->finalize();
+        DevBuf<double> tmp;
+        tmp.alloc(d->n_interior * (u ? 4 : 1), "cudaMalloc(moments)");
+        d->ops->moments(d->dev, d->steps, tmp.p, u ? tmp.p + d->n_interior : nullptr, d->stream);
+        check(cudaGetLastError(), "moments kernel");
+        check(cudaMemcpyAsync(rho, tmp.p, d->n_interior * sizeof(double), cudaMemcpyDeviceToHost, d->stream),
+              "download density");
+        if (u)
+            check(cudaMemcpyAsync(u, tmp.p + d->n_interior, 3 * d->n_interior * sizeof(double),
+                                  cudaMemcpyDeviceToHost, d->stream),
+                  "download velocity");
+        check(cudaStreamSynchronize(d->stream), "moments");
+    });
+}
+
+int lbm_reduce_mass_momentum(lbm_domain* d, double out[4])
+{
+    bool diverged = false;
+    const int rc = guarded(d, [&] {
+        if (!out) throw ArgError("out is NULL");
+        d->finalize();
+        double* partials = d->red.p;
+        double* total = d->red.p + 4 * kReduceBlocks;
+        d->ops->reduce(d->dev, d->steps, partials, kReduceBlocks, total, d->stream);
+        check(cudaGetLastError(), "reduction kernel");
+        check(cudaMemcpyAsync(out, total, 4 * sizeof(double), cudaMemcpyDeviceToHost, d->stream), "download totals");
+        check(cudaStreamSynchronize(d->stream), "reduction");
+        for (int k = 0; k < 4; ++k) diverged = diverged || !std::isfinite(out[k]);
+        if (diverged) d->err = "non-finite mass or momentum: the run diverged";
+    });
+    if (rc == LBM_OK && diverged) return LBM_ERR_DIVERGED;
+    return rc;
+}
+
+int lbm_sync(lbm_domain* d)
+{
+    return guarded(d, [&] { check(cudaStreamSynchronize(d->stream), "cudaStreamSynchronize"); });
+}
+
+int lbm_get_stream(lbm_domain* d, void** stream)
+{
+    return guarded(d, [&] {
+        if (!stream) throw ArgError("stream is NULL");
+        *stream = static_cast<void*>(d->stream);
+    });
+}
+
+int64_t lbm_steps_done(const lbm_domain* d) { return d ? d->steps : -1; }
+
+int lbm_memory_info(const lbm_domain* d, uint64_t* device_bytes, uint64_t* step_bytes, uint64_t* fluid_cells)
+{
+    if (!d) return LBM_ERR_ARG;
+    lbm_domain* m = const_cast<lbm_domain*>(d);
+    return guarded(m, [&] {
+        m->finalize();
+        if (device_bytes)
+            *device_bytes = m->pop.bytes() + m->flag.bytes() + m->bc.bytes() + m->profile.bytes() + m->gf_xyz.bytes() +
+                            m->gf_pop.bytes() + m->fs_link.bytes() + m->red.bytes();
+        if (step_bytes) *step_bytes = 2ull * m->Q * store_bytes(m->precision) * m->fluid_cells;
+        if (fluid_cells) *fluid_cells = m->fluid_cells;
+    });
+}
+
+const char* lbm_last_error(const lbm_domain* d)
+{
+    if (!d) return g_create_error.c_str();
+    return d->err.c_str();
+}
+
+}  // extern "C"

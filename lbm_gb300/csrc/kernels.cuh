@@ -1,0 +1,453 @@
+// Device kernels of the lattice Boltzmann step, templated on the lattice model L and the
+// population storage type S. Each step_*.cu translation unit includes this file and
+// instantiates it for one storage type (step_fp64.cu is compiled with -fmad=false so that the
+// FP64 path performs every operation the reference performs, in the same order, unfused).
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include "domain.cuh"
+#include "lattice.cuh"
+
+namespace lbmg {
+
+// ------------------------------------------------------------------------------------------
+// Storage policies. FP64 stores populations as they are and computes in FP64 exactly as the
+// reference does. The other stores hold s_q = f_q - w_q and compute in FP32 on s directly, so
+// the O(1) part of every population never enters the rounding.
+// ------------------------------------------------------------------------------------------
+template <class S>
+struct Store;
+
+template <>
+struct Store<double> {
+    using C = double;
+    static constexpr bool kShifted = false;
+    __device__ static __forceinline__ double ld(const double* p) { return *p; }
+    __device__ static __forceinline__ void st(double* p, double v) { *p = v; }
+};
+template <>
+struct Store<float> {
+    using C = float;
+    static constexpr bool kShifted = true;
+    __device__ static __forceinline__ float ld(const float* p) { return *p; }
+    __device__ static __forceinline__ void st(float* p, float v) { *p = v; }
+};
+template <>
+struct Store<__half> {
+    using C = float;
+    static constexpr bool kShifted = true;
+    __device__ static __forceinline__ float ld(const __half* p) { return __half2float(*p); }
+    __device__ static __forceinline__ void st(__half* p, float v) { *p = __float2half_rn(v); }
+};
+template <>
+struct Store<__nv_bfloat16> {
+    using C = float;
+    static constexpr bool kShifted = true;
+    __device__ static __forceinline__ float ld(const __nv_bfloat16* p)
+    {
+        return __bfloat162float(*p);
+    }
+    __device__ static __forceinline__ void st(__nv_bfloat16* p, float v)
+    {
+        *p = __float2bfloat16_rn(v);
+    }
+};
+
+// Storage value <-> FP64 population f_q.
+template <class L, class S>
+__device__ __forceinline__ double to_f64(typename Store<S>::C v, int q)
+{
+    if constexpr (Store<S>::kShifted)
+        return L::w(q) + static_cast<double>(v);
+    else
+        return static_cast<double>(v);
+}
+template <class L, class S>
+__device__ __forceinline__ typename Store<S>::C from_f64(double f, int q)
+{
+    if constexpr (Store<S>::kShifted)
+        return static_cast<float>(f - L::w(q));
+    else
+        return f;
+}
+
+// ------------------------------------------------------------------------------------------
+// Indexing.
+// ------------------------------------------------------------------------------------------
+__device__ __forceinline__ int cidx(const Geom& g, int x, int y, int z)
+{
+    return kXOff + x + g.XS * (y + g.YS * z);
+}
+
+__device__ __forceinline__ int wrap_axis(int v, int l, bool per)
+{
+    if (per) {
+        if (v < 1) v += l;
+        else if (v > l) v -= l;
+    }
+    return v;
+}
+
+// Neighbour (x+dx, y+dy, z+dz) with periodic wrap; writes its coordinates.
+__device__ __forceinline__ void nbr_xyz(const Geom& g, int x, int y, int z, int dx, int dy,
+                                        int dz, int& nx, int& ny, int& nz)
+{
+    nx = wrap_axis(x + dx, g.xl, g.per & 1);
+    ny = wrap_axis(y + dy, g.yl, g.per & 2);
+    nz = wrap_axis(z + dz, g.zl, g.per & 4);
+}
+
+__device__ __forceinline__ bool interior(const Geom& g, int x, int y, int z)
+{
+    return x >= 1 && x <= g.xl && y >= 1 && y <= g.yl && z >= 1 && z <= g.zl;
+}
+
+// Reference cell order (domain.hpp:60-64) for host-facing arrays.
+__device__ __forceinline__ size_t ref_idx(const Geom& g, int x, int y, int z)
+{
+    return static_cast<size_t>(x) +
+           static_cast<size_t>(g.xl + 2) *
+               (static_cast<size_t>(y) + static_cast<size_t>(g.yl + 2) * static_cast<size_t>(z));
+}
+
+__device__ __forceinline__ bool is_fluid(uint8_t f) { return f <= kFluidEdge; }
+
+// ------------------------------------------------------------------------------------------
+// FP64 arithmetic in the reference's operation order (collision.hpp:6-70, boundary.hpp).
+// Multiplications by a lattice velocity component c in {-1, 0, 1} are written as an add, a
+// subtract or nothing: x*1 = x, x*(-1) = -x and x + (+-0) = x for the running sums here (they
+// start at +0.0 and can never be -0.0), so the results are bit-identical.
+// ------------------------------------------------------------------------------------------
+template <class L>
+__device__ __forceinline__ double density_exact(const double (&f)[L::Q])
+{
+    double rho = 0.0;
+#pragma unroll
+    for (int q = 0; q < L::Q; ++q) rho += f[q];
+    return rho;
+}
+
+// Momentum sum_q f_q c_qd (d outer, q inner: collision.hpp:19-24), before the division.
+template <class L>
+__device__ __forceinline__ double momentum_exact(const double (&f)[L::Q], int d)
+{
+    double s = 0.0;
+#pragma unroll
+    for (int q = 0; q < L::Q; ++q) {
+        const int c = L::c(q, d);
+        if (c > 0) s += f[q];
+        else if (c < 0) s -= f[q];
+    }
+    return s;
+}
+
+// compute_feq (collision.hpp:33-51) for one direction q.
+template <class L>
+__device__ __forceinline__ double feq_exact(int q, double rho, double u0, double u1, double u2)
+{
+    double cu = 0.0;
+    double uu = 0.0;
+    const int c0 = L::c(q, 0), c1 = L::c(q, 1), c2 = L::c(q, 2);
+    if (c0 > 0) cu += u0; else if (c0 < 0) cu -= u0;
+    uu += u0 * u0;
+    if (c1 > 0) cu += u1; else if (c1 < 0) cu -= u1;
+    uu += u1 * u1;
+    if (c2 > 0) cu += u2; else if (c2 < 0) cu -= u2;
+    uu += u2 * u2;
+    return L::w(q) * rho * (1 + cu / kCS2 + (cu) * (cu) / kCS4x2 - uu / kCS2x2);
+}
+
+// BGKCollision::collide (collision.hpp:60-70).
+template <class L>
+__device__ __forceinline__ void collide_exact(double (&f)[L::Q], double tau)
+{
+    const double rho = density_exact<L>(f);
+    const double u0 = momentum_exact<L>(f, 0) / rho;
+    const double u1 = momentum_exact<L>(f, 1) / rho;
+    const double u2 = momentum_exact<L>(f, 2) / rho;
+#pragma unroll
+    for (int q = 0; q < L::Q; ++q) {
+        const double feq = feq_exact<L>(q, rho, u0, u1, u2);
+        f[q] -= (f[q] - feq) / tau;
+    }
+}
+
+// Value a boundary cell's handler writes into its direction q = inv(p) for the fluid cell that
+// sees it in direction p, from that fluid cell's post-collision populations fs
+// (boundary.hpp:14-214). rho_s = density_exact(fs).
+template <class L>
+__device__ __forceinline__ double bc_value_exact(const BcEntry& b, int p, const double (&fs)[L::Q],
+                                                 double rho_s, const double* vcell)
+{
+    const int q = inv<L>(p);
+    switch (b.type) {
+    case kMovingWall: {  // boundary.hpp:52-66
+        double cu = 0.0;
+        const int c0 = L::c(q, 0), c1 = L::c(q, 1), c2 = L::c(q, 2);
+        if (c0 > 0) cu += b.v[0]; else if (c0 < 0) cu -= b.v[0];
+        if (c1 > 0) cu += b.v[1]; else if (c1 < 0) cu -= b.v[1];
+        if (c2 > 0) cu += b.v[2]; else if (c2 < 0) cu -= b.v[2];
+        const double finv = fs[p];
+        return finv + 2.0 * L::w(q) * rho_s * cu / kCS2;
+    }
+    case kInflow: {  // boundary.hpp:173-179
+        const double* v = vcell ? vcell : b.v;
+        return feq_exact<L>(q, b.rho, v[0], v[1], v[2]);
+    }
+    case kOutflow:     // boundary.hpp:137-148
+    case kPressure: {  // boundary.hpp:203-212
+        const double u0 = momentum_exact<L>(fs, 0) / b.rho;
+        const double u1 = momentum_exact<L>(fs, 1) / b.rho;
+        const double u2 = momentum_exact<L>(fs, 2) / b.rho;
+        return feq_exact<L>(q, b.rho, u0, u1, u2) + feq_exact<L>(p, b.rho, u0, u1, u2) - fs[p];
+    }
+    default:  // kNoSlip, boundary.hpp:22-29
+        return fs[p];
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// FP32 arithmetic on shifted populations s_q = f_q - w_q. With rho = 1 + drho,
+//   f_eq,q - w_q = w_q (drho + rho (cu/cs2 + cu^2/(2 cs4) - uu/(2 cs2)))
+// keeps the reference's truncated speed of sound (collision.hpp:45-46).
+// ------------------------------------------------------------------------------------------
+constexpr float kA = static_cast<float>(1.0 / kCS2);
+constexpr float kB = static_cast<float>(1.0 / kCS4x2);
+constexpr float kC = static_cast<float>(1.0 / kCS2x2);
+
+template <class L>
+__device__ __forceinline__ float seq_shifted(int q, float drho, float rho, float ux, float uy,
+                                             float uz, float uu_c)
+{
+    const float cu = L::c(q, 0) * ux + L::c(q, 1) * uy + L::c(q, 2) * uz;
+    return static_cast<float>(L::w(q)) * (drho + rho * (cu * (kA + cu * kB) - uu_c));
+}
+
+template <class L>
+__device__ __forceinline__ void moments_shifted(const float (&s)[L::Q], float& drho, float& jx,
+                                                float& jy, float& jz)
+{
+    drho = 0.f; jx = 0.f; jy = 0.f; jz = 0.f;
+#pragma unroll
+    for (int q = 0; q < L::Q; ++q) {
+        drho += s[q];
+        if (L::c(q, 0) > 0) jx += s[q]; else if (L::c(q, 0) < 0) jx -= s[q];
+        if (L::c(q, 1) > 0) jy += s[q]; else if (L::c(q, 1) < 0) jy -= s[q];
+        if (L::c(q, 2) > 0) jz += s[q]; else if (L::c(q, 2) < 0) jz -= s[q];
+    }
+}
+
+template <class L>
+__device__ __forceinline__ void collide_shifted(float (&s)[L::Q], float omega)
+{
+    float drho, jx, jy, jz;
+    moments_shifted<L>(s, drho, jx, jy, jz);
+    const float rho = 1.f + drho;
+    const float ir = 1.f / rho;
+    const float ux = jx * ir, uy = jy * ir, uz = jz * ir;
+    const float uu_c = (ux * ux + uy * uy + uz * uz) * kC;
+#pragma unroll
+    for (int q = 0; q < L::Q; ++q) {
+        const float seq = seq_shifted<L>(q, drho, rho, ux, uy, uz, uu_c);
+        s[q] = fmaf(omega, seq - s[q], s[q]);
+    }
+}
+
+template <class L>
+__device__ __forceinline__ float bc_value_shifted(const BcEntry& b, int p, const float (&ss)[L::Q],
+                                                  float drho_s, float jx, float jy, float jz,
+                                                  const double* vcell)
+{
+    const int q = inv<L>(p);
+    switch (b.type) {
+    case kMovingWall: {
+        const float rho = 1.f + drho_s;
+        const float cu = L::c(q, 0) * static_cast<float>(b.v[0]) +
+                         L::c(q, 1) * static_cast<float>(b.v[1]) +
+                         L::c(q, 2) * static_cast<float>(b.v[2]);
+        return ss[p] + 2.f * static_cast<float>(L::w(q)) * rho * cu * kA;
+    }
+    case kInflow: {
+        const double* v = vcell ? vcell : b.v;
+        const float r = static_cast<float>(b.rho);
+        const float ux = static_cast<float>(v[0]), uy = static_cast<float>(v[1]),
+                    uz = static_cast<float>(v[2]);
+        return seq_shifted<L>(q, r - 1.f, r, ux, uy, uz, (ux * ux + uy * uy + uz * uz) * kC);
+    }
+    case kOutflow:
+    case kPressure: {
+        const float r = static_cast<float>(b.rho);
+        const float ir = 1.f / r;
+        const float ux = jx * ir, uy = jy * ir, uz = jz * ir;
+        const float uu_c = (ux * ux + uy * uy + uz * uz) * kC;
+        return seq_shifted<L>(q, r - 1.f, r, ux, uy, uz, uu_c) +
+               seq_shifted<L>(p, r - 1.f, r, ux, uy, uz, uu_c) - ss[p];
+    }
+    default:
+        return ss[p];
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// The fused time step: pull-stream + BGK collide + boundary handlers, one thread per interior
+// cell, in place (AA pattern). ODD = the step number (1-based) is odd, i.e. the populations are
+// pulled from the neighbours; even steps read and write the cell's own slots.
+// ------------------------------------------------------------------------------------------
+template <class S>
+struct StepParams {
+    S* pop;
+    const uint8_t* flag;
+    const BcEntry* bc;
+    const double* profile;
+    Geom g;
+    double tau;
+    float omega;
+};
+
+template <class L, class S, bool ODD>
+__global__ void __launch_bounds__(kBlockX) step_kernel(const StepParams<S> P)
+{
+    using St = Store<S>;
+    using T = typename St::C;
+    constexpr int Q = L::Q;
+    const int x = 1 + static_cast<int>(blockIdx.x) * kBlockX + static_cast<int>(threadIdx.x);
+    if (x > P.g.xl) return;
+    const int y = 1 + static_cast<int>(blockIdx.y);
+    const int z = 1 + static_cast<int>(blockIdx.z);
+    const int i = cidx(P.g, x, y, z);
+    const uint8_t fl = P.flag[i];
+    if (fl > kFluidEdge) return;
+
+    S* __restrict__ pop = P.pop;
+    const size_t PS = P.g.PS;
+    const int sy = P.g.XS;
+    const int sz = P.g.XS * P.g.YS;
+    T f[Q];
+
+    if (fl == kFluidBulk) {
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            const int off = L::c(q, 0) + L::c(q, 1) * sy + L::c(q, 2) * sz;
+            f[q] = ODD ? St::ld(pop + static_cast<size_t>(inv<L>(q)) * PS + (i - off))
+                       : St::ld(pop + static_cast<size_t>(q) * PS + i);
+        }
+    } else {
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            if (ODD) {
+                int nx, ny, nz;
+                nbr_xyz(P.g, x, y, z, -L::c(q, 0), -L::c(q, 1), -L::c(q, 2), nx, ny, nz);
+                const int n = cidx(P.g, nx, ny, nz);
+                f[q] = is_fluid(P.flag[n]) ? St::ld(pop + static_cast<size_t>(inv<L>(q)) * PS + n)
+                                           : St::ld(pop + static_cast<size_t>(q) * PS + i);
+            } else {
+                f[q] = St::ld(pop + static_cast<size_t>(q) * PS + i);
+            }
+        }
+    }
+
+    if constexpr (St::kShifted)
+        collide_shifted<L>(f, P.omega);
+    else
+        collide_exact<L>(f, P.tau);
+
+    if (fl == kFluidBulk) {
+#pragma unroll
+        for (int p = 0; p < Q; ++p) {
+            const int off = L::c(p, 0) + L::c(p, 1) * sy + L::c(p, 2) * sz;
+            if (ODD)
+                St::st(pop + static_cast<size_t>(p) * PS + (i + off), f[p]);
+            else
+                St::st(pop + static_cast<size_t>(inv<L>(p)) * PS + i, f[p]);
+        }
+        return;
+    }
+
+    // Edge cell: moments of the post-collision state for the handlers that need them.
+    T m0, m1, m2, m3;
+    if constexpr (St::kShifted) {
+        moments_shifted<L>(f, m0, m1, m2, m3);
+    } else {
+        m0 = density_exact<L>(f);
+        m1 = m2 = m3 = 0.0;
+    }
+#pragma unroll
+    for (int p = 0; p < Q; ++p) {
+        int mx, my, mz;
+        nbr_xyz(P.g, x, y, z, L::c(p, 0), L::c(p, 1), L::c(p, 2), mx, my, mz);
+        const int m = cidx(P.g, mx, my, mz);
+        const uint8_t flm = P.flag[m];
+        if (is_fluid(flm)) {
+            if (ODD)
+                St::st(pop + static_cast<size_t>(p) * PS + m, f[p]);
+            else
+                St::st(pop + static_cast<size_t>(inv<L>(p)) * PS + i, f[p]);
+            continue;
+        }
+        // Not fluid: keep the raw post-collision value in the neighbour's slot (read back by
+        // lbm_get_populations / lbm_moments) and store the handler's value where this cell
+        // pulls direction inv(p) next step.
+        St::st(pop + static_cast<size_t>(p) * PS + m, f[p]);
+        if (flm < kFirstHandler) continue;  // ghost-fluid neighbour: side pass fills the slot
+        const BcEntry& b = P.bc[flm - kFirstHandler];
+        if (b.type == kFreeSlip) continue;  // free-slip side pass fills the slot
+        const double* vcell = nullptr;
+        if (b.type == kInflow && b.has_profile) vcell = P.profile + 3 * ref_idx(P.g, mx, my, mz);
+        T val;
+        if constexpr (St::kShifted)
+            val = bc_value_shifted<L>(b, p, f, m0, m1, m2, m3, vcell);
+        else
+            val = bc_value_exact<L>(b, p, f, m0, vcell);
+        St::st(pop + static_cast<size_t>(inv<L>(p)) * PS + i, val);
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// Reading the state back in the reference's terms.
+// ------------------------------------------------------------------------------------------
+
+// Post-collision population p of interior fluid cell (x, y, z) at layout index i, after a
+// number of steps whose parity is `odd`.
+template <class L, class S>
+__device__ __forceinline__ typename Store<S>::C load_post(const S* pop, const uint8_t* flag,
+                                                          const Geom& g, int x, int y, int z,
+                                                          int i, int p, bool odd)
+{
+    int mx, my, mz;
+    nbr_xyz(g, x, y, z, L::c(p, 0), L::c(p, 1), L::c(p, 2), mx, my, mz);
+    const int m = cidx(g, mx, my, mz);
+    if (!odd && is_fluid(flag[m])) return Store<S>::ld(pop + static_cast<size_t>(inv<L>(p)) * g.PS + i);
+    return Store<S>::ld(pop + static_cast<size_t>(p) * g.PS + m);
+}
+
+// collide_field populations of any cell as FP64 (see lbm_get_populations). Ghost-fluid cells
+// come out as w_q here; the caller overwrites them from the side copies.
+template <class L, class S>
+__device__ __forceinline__ void load_cell_f64(const S* pop, const uint8_t* flag, const Geom& g,
+                                              int x, int y, int z, bool odd, double (&out)[L::Q])
+{
+    const int i = cidx(g, x, y, z);
+    const uint8_t fl = flag[i];
+    if (is_fluid(fl) && interior(g, x, y, z)) {
+#pragma unroll
+        for (int p = 0; p < L::Q; ++p)
+            out[p] = to_f64<L, S>(load_post<L, S>(pop, flag, g, x, y, z, i, p, odd), p);
+        return;
+    }
+#pragma unroll
+    for (int q = 0; q < L::Q; ++q) {
+        int nx, ny, nz;
+        nbr_xyz(g, x, y, z, L::c(q, 0), L::c(q, 1), L::c(q, 2), nx, ny, nz);
+        double v = L::w(q);
+        if (fl >= kFirstHandler && interior(g, nx, ny, nz)) {
+            const int n = cidx(g, nx, ny, nz);
+            if (is_fluid(flag[n]))
+                v = to_f64<L, S>(Store<S>::ld(pop + static_cast<size_t>(q) * g.PS + n), q);
+        }
+        out[q] = v;
+    }
+}
+
+}  // namespace lbmg

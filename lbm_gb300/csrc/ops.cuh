@@ -1,0 +1,38 @@
+// Per-(lattice, storage precision) kernel launchers, reached through a table of function
+// pointers so that the host layer (capi.cu) stays free of templates and each precision lives in
+// its own translation unit.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "domain.cuh"
+
+namespace lbmg {
+
+struct KernelOps {
+    // all planes <- initial weights
+    void (*init)(const DomainDev& d, cudaStream_t s);
+    // fluid cells -> kFluidBulk / kFluidEdge
+    void (*classify)(const DomainDev& d, cudaStream_t s);
+    // one time step number `t` (1-based): fused kernel, then the side passes
+    void (*step)(const DomainDev& d, long long t, cudaStream_t s);
+    // state after `k` steps -> AoS FP64 over all cells (device buffer)
+    void (*gather)(const DomainDev& d, long long k, double* out, cudaStream_t s);
+    // AoS FP64 over all cells (device buffer) -> state after `k` steps
+    void (*scatter)(const DomainDev& d, long long k, const double* in, cudaStream_t s);
+    // interior moments (device buffers)
+    void (*moments)(const DomainDev& d, long long k, double* rho, double* u, cudaStream_t s);
+    // FP64 totals into out[4] (device), partials: scratch of 4 * reduce_blocks doubles
+    void (*reduce)(const DomainDev& d, long long k, double* partials, int reduce_blocks,
+                   double* out, cudaStream_t s);
+};
+
+const KernelOps* ops_fp64(int q);
+const KernelOps* ops_fp32(int q);
+const KernelOps* ops_fp16(int q);
+const KernelOps* ops_bf16(int q);
+
+// Blocks used by the reduction: a fixed grid, so the summation order never changes.
+constexpr int kReduceBlocks = 4 * 152;
+
+}  // namespace lbmg

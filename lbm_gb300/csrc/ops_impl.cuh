@@ -1,0 +1,130 @@
+// Launcher bodies for one storage type S; included by step_fp64.cu, step_fp32.cu, step_fp16.cu
+// and step_bf16.cu, each of which defines LBMG_STORE and LBMG_OPS_NAME before including it.
+#pragma once
+
+#include "ops.cuh"
+#include "state_kernels.cuh"
+
+namespace lbmg {
+namespace {
+
+inline dim3 cell_grid(const Geom& g)
+{
+    return dim3(static_cast<unsigned>((g.xl + kBlockX - 1) / kBlockX), static_cast<unsigned>(g.yl),
+                static_cast<unsigned>(g.zl));
+}
+
+inline unsigned linear_blocks(size_t n, unsigned threads)
+{
+    const size_t b = (n + threads - 1) / threads;
+    return static_cast<unsigned>(b < 65535u * 16u ? (b > 0 ? b : 1) : 65535u * 16u);
+}
+
+template <class S>
+StepParams<S> step_params(const DomainDev& d)
+{
+    StepParams<S> p;
+    p.pop = static_cast<S*>(d.pop);
+    p.flag = d.flag;
+    p.bc = d.bc;
+    p.profile = d.profile;
+    p.g = d.g;
+    p.tau = d.tau;
+    p.omega = static_cast<float>(1.0 / d.tau);
+    return p;
+}
+
+template <int Q, class S>
+struct Launch {
+    using L = Lattice<Q>;
+
+    static void init(const DomainDev& d, cudaStream_t s)
+    {
+        init_kernel<L, S><<<linear_blocks(Q * d.g.PS, 256), 256, 0, s>>>(static_cast<S*>(d.pop), d.g.PS);
+    }
+
+    static void classify(const DomainDev& d, cudaStream_t s)
+    {
+        classify_kernel<L><<<cell_grid(d.g), kBlockX, 0, s>>>(d.flag, d.g);
+    }
+
+    static void side_passes(const DomainDev& d, long long k, cudaStream_t s)
+    {
+        const int copy = static_cast<int>(k & 1);
+        S* pop = static_cast<S*>(d.pop);
+        if (d.n_gf > 0)
+            ghost_fluid_kernel<L, S><<<(d.n_gf + 127) / 128, 128, 0, s>>>(
+                pop, d.flag, d.g, d.tau, d.gf_xyz, d.gf_pop, d.n_gf, copy);
+        if (d.n_fs > 0)
+            free_slip_kernel<L, S><<<(d.n_fs + 127) / 128, 128, 0, s>>>(
+                pop, d.flag, d.g, d.fs_link, d.n_fs, copy, d.gf_pop, d.n_gf, copy);
+    }
+
+    static void step(const DomainDev& d, long long t, cudaStream_t s)
+    {
+        const StepParams<S> p = step_params<S>(d);
+        if (t & 1)
+            step_kernel<L, S, true><<<cell_grid(d.g), kBlockX, 0, s>>>(p);
+        else
+            step_kernel<L, S, false><<<cell_grid(d.g), kBlockX, 0, s>>>(p);
+        side_passes(d, t, s);
+    }
+
+    static void gather(const DomainDev& d, long long k, double* out, cudaStream_t s)
+    {
+        const size_t ng = static_cast<size_t>(d.g.xl + 2) * (d.g.yl + 2) * (d.g.zl + 2);
+        gather_kernel<L, S><<<linear_blocks(ng, 256), 256, 0, s>>>(
+            static_cast<const S*>(d.pop), d.flag, d.g, static_cast<int>(k & 1), out);
+        if (d.n_gf > 0)
+            ghost_fluid_io_kernel<L><<<(d.n_gf + 127) / 128, 128, 0, s>>>(
+                d.g, d.gf_xyz, d.gf_pop, d.n_gf, static_cast<int>(k & 1), out, 1);
+    }
+
+    static void scatter(const DomainDev& d, long long k, const double* in, cudaStream_t s)
+    {
+        S* pop = static_cast<S*>(d.pop);
+        scatter_kernel<L, S><<<cell_grid(d.g), kBlockX, 0, s>>>(pop, d.flag, d.g,
+                                                                static_cast<int>(k & 1), in);
+        if (d.n_gf > 0) {
+            const int copy = static_cast<int>(k & 1);
+            ghost_fluid_io_kernel<L><<<(d.n_gf + 127) / 128, 128, 0, s>>>(
+                d.g, d.gf_xyz, d.gf_pop, d.n_gf, copy, const_cast<double*>(in), 0);
+            ghost_fluid_slots_kernel<L, S><<<(d.n_gf + 127) / 128, 128, 0, s>>>(
+                pop, d.flag, d.g, d.gf_xyz, d.gf_pop, d.n_gf, copy);
+        }
+    }
+
+    static void moments(const DomainDev& d, long long k, double* rho, double* u, cudaStream_t s)
+    {
+        moments_kernel<L, S><<<cell_grid(d.g), kBlockX, 0, s>>>(
+            static_cast<const S*>(d.pop), d.flag, d.g, static_cast<int>(k & 1), rho, u);
+    }
+
+    static void reduce(const DomainDev& d, long long k, double* partials, int nblocks,
+                       double* out, cudaStream_t s)
+    {
+        reduce_kernel<L, S><<<nblocks, kReduceThreads, 0, s>>>(
+            static_cast<const S*>(d.pop), d.flag, d.g, static_cast<int>(k & 1), partials);
+        reduce_final_kernel<<<1, 32, 0, s>>>(partials, nblocks, out);
+    }
+
+    static const KernelOps* table()
+    {
+        static const KernelOps t = {&init, &classify, &step, &gather, &scatter, &moments, &reduce};
+        return &t;
+    }
+};
+
+}  // namespace
+
+const KernelOps* LBMG_OPS_NAME(int q)
+{
+    switch (q) {
+    case 15: return Launch<15, LBMG_STORE>::table();
+    case 19: return Launch<19, LBMG_STORE>::table();
+    case 27: return Launch<27, LBMG_STORE>::table();
+    default: return nullptr;
+    }
+}
+
+}  // namespace lbmg

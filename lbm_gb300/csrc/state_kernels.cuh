@@ -1,0 +1,264 @@
+// Kernels around the time step: initialisation, cell classification, conversion between the
+// in-place device layout and the reference's AoS population field, moments, the FP64
+// conservation reduction, and the two side passes (ghost-fluid cells, free-slip links).
+#pragma once
+
+#include "kernels.cuh"
+
+namespace lbmg {
+
+// Every plane q holds w_q (FP64 store) or 0 (shifted stores): the reference's initial state
+// (cell.hpp:8-15) in any layout parity and for any geometry, boundary slots included.
+template <class L, class S>
+__global__ void init_kernel(S* pop, size_t PS)
+{
+    const size_t n = static_cast<size_t>(L::Q) * PS;
+    for (size_t k = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; k < n;
+         k += static_cast<size_t>(gridDim.x) * blockDim.x) {
+        const int q = static_cast<int>(k / PS);
+        Store<S>::st(pop + k, from_f64<L, S>(L::w(q), q));
+    }
+}
+
+// Interior fluid cells: kFluidEdge when some neighbour is not fluid or lies across a periodic
+// wrap, else kFluidBulk. The lattice is symmetric, so checking x + c_q for all q covers both the
+// pull (x - c_q) and the push (x + c_q) neighbours.
+template <class L>
+__global__ void classify_kernel(uint8_t* flag, Geom g)
+{
+    const int x = 1 + static_cast<int>(blockIdx.x) * kBlockX + static_cast<int>(threadIdx.x);
+    if (x > g.xl) return;
+    const int y = 1 + static_cast<int>(blockIdx.y), z = 1 + static_cast<int>(blockIdx.z);
+    const int i = cidx(g, x, y, z);
+    if (!is_fluid(flag[i])) return;
+    bool edge = false;
+#pragma unroll
+    for (int q = 0; q < L::Q; ++q) {
+        const int ax = x + L::c(q, 0), ay = y + L::c(q, 1), az = z + L::c(q, 2);
+        int nx, ny, nz;
+        nbr_xyz(g, x, y, z, L::c(q, 0), L::c(q, 1), L::c(q, 2), nx, ny, nz);
+        if (nx != ax || ny != ay || nz != az) edge = true;
+        // flags of fluid cells only move between kFluidBulk and kFluidEdge here, so this read
+        // of a neighbour's flag sees the same fluid / non-fluid answer whatever the timing
+        if (!is_fluid(flag[cidx(g, nx, ny, nz)])) edge = true;
+    }
+    flag[i] = edge ? kFluidEdge : kFluidBulk;
+}
+
+// Device layout -> AoS FP64 field over all cells (reference cell order).
+template <class L, class S>
+__global__ void gather_kernel(const S* pop, const uint8_t* flag, Geom g, int odd, double* out)
+{
+    const size_t ng = static_cast<size_t>(g.xl + 2) * (g.yl + 2) * (g.zl + 2);
+    for (size_t r = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; r < ng;
+         r += static_cast<size_t>(gridDim.x) * blockDim.x) {
+        const int x = static_cast<int>(r % (g.xl + 2));
+        const int y = static_cast<int>((r / (g.xl + 2)) % (g.yl + 2));
+        const int z = static_cast<int>(r / (static_cast<size_t>(g.xl + 2) * (g.yl + 2)));
+        double f[L::Q];
+        load_cell_f64<L, S>(pop, flag, g, x, y, z, odd != 0, f);
+#pragma unroll
+        for (int q = 0; q < L::Q; ++q) out[r * L::Q + q] = f[q];
+    }
+}
+
+// AoS FP64 field (reference order) -> device layout with the given parity. One thread per
+// interior fluid cell writes its own post-collision slots and the boundary slots it pulls from.
+template <class L, class S>
+__global__ void scatter_kernel(S* pop, const uint8_t* flag, Geom g, int odd, const double* in)
+{
+    const int x = 1 + static_cast<int>(blockIdx.x) * kBlockX + static_cast<int>(threadIdx.x);
+    if (x > g.xl) return;
+    const int y = 1 + static_cast<int>(blockIdx.y), z = 1 + static_cast<int>(blockIdx.z);
+    const int i = cidx(g, x, y, z);
+    if (!is_fluid(flag[i])) return;
+    const size_t r = ref_idx(g, x, y, z);
+#pragma unroll
+    for (int p = 0; p < L::Q; ++p) {
+        int mx, my, mz;
+        nbr_xyz(g, x, y, z, L::c(p, 0), L::c(p, 1), L::c(p, 2), mx, my, mz);
+        const int m = cidx(g, mx, my, mz);
+        const auto v = from_f64<L, S>(in[r * L::Q + p], p);
+        if (!odd && is_fluid(flag[m]))
+            Store<S>::st(pop + static_cast<size_t>(inv<L>(p)) * g.PS + i, v);
+        else
+            Store<S>::st(pop + static_cast<size_t>(p) * g.PS + m, v);
+    }
+#pragma unroll
+    for (int q = 0; q < L::Q; ++q) {
+        int nx, ny, nz;
+        nbr_xyz(g, x, y, z, -L::c(q, 0), -L::c(q, 1), -L::c(q, 2), nx, ny, nz);
+        const int n = cidx(g, nx, ny, nz);
+        if (is_fluid(flag[n])) continue;
+        const auto v = from_f64<L, S>(in[ref_idx(g, nx, ny, nz) * L::Q + q], q);
+        Store<S>::st(pop + static_cast<size_t>(q) * g.PS + i, v);
+    }
+}
+
+// Density and velocity of interior cells (vtk.hpp:62-73 -> collision.hpp:6-31), FP64, written
+// as rho[n] and u[3n..3n+2] in interior order.
+template <class L, class S>
+__global__ void moments_kernel(const S* pop, const uint8_t* flag, Geom g, int odd,
+                               double* rho_out, double* u_out)
+{
+    const int x = 1 + static_cast<int>(blockIdx.x) * kBlockX + static_cast<int>(threadIdx.x);
+    if (x > g.xl) return;
+    const int y = 1 + static_cast<int>(blockIdx.y), z = 1 + static_cast<int>(blockIdx.z);
+    double f[L::Q];
+    load_cell_f64<L, S>(pop, flag, g, x, y, z, odd != 0, f);
+    const double rho = density_exact<L>(f);
+    const size_t n = static_cast<size_t>(x - 1) +
+                     static_cast<size_t>(g.xl) * (static_cast<size_t>(y - 1) +
+                                                  static_cast<size_t>(g.yl) * (z - 1));
+    rho_out[n] = rho;
+    if (u_out) {
+        u_out[3 * n + 0] = momentum_exact<L>(f, 0) / rho;
+        u_out[3 * n + 1] = momentum_exact<L>(f, 1) / rho;
+        u_out[3 * n + 2] = momentum_exact<L>(f, 2) / rho;
+    }
+}
+
+// FP64 totals {sum rho, sum j} over interior fluid cells. Each block writes one partial into
+// `partials` (4 doubles per block); reduce_final_kernel adds them in block order, so the result
+// does not depend on scheduling.
+constexpr int kReduceThreads = 256;
+
+template <class L, class S>
+__global__ void __launch_bounds__(kReduceThreads)
+    reduce_kernel(const S* pop, const uint8_t* flag, Geom g, int odd, double* partials)
+{
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    const size_t n = static_cast<size_t>(g.xl) * g.yl * g.zl;
+    for (size_t k = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; k < n;
+         k += static_cast<size_t>(gridDim.x) * blockDim.x) {
+        const int x = 1 + static_cast<int>(k % g.xl);
+        const int y = 1 + static_cast<int>((k / g.xl) % g.yl);
+        const int z = 1 + static_cast<int>(k / (static_cast<size_t>(g.xl) * g.yl));
+        const int i = cidx(g, x, y, z);
+        if (!is_fluid(flag[i])) continue;
+#pragma unroll
+        for (int p = 0; p < L::Q; ++p) {
+            const double f = to_f64<L, S>(load_post<L, S>(pop, flag, g, x, y, z, i, p, odd != 0), p);
+            acc[0] += f;
+            acc[1] += L::c(p, 0) * f;
+            acc[2] += L::c(p, 1) * f;
+            acc[3] += L::c(p, 2) * f;
+        }
+    }
+    __shared__ double red[4][kReduceThreads / 32];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        double v = acc[k];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if ((threadIdx.x & 31) == 0) red[k][threadIdx.x >> 5] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 4) {
+        double v = 0.0;
+        for (int w = 0; w < kReduceThreads / 32; ++w) v += red[threadIdx.x][w];
+        partials[4 * blockIdx.x + threadIdx.x] = v;
+    }
+}
+
+static __global__ void reduce_final_kernel(const double* partials, int nblocks, double* out)
+{
+    if (threadIdx.x < 4) {
+        double v = 0.0;
+        for (int b = 0; b < nblocks; ++b) v += partials[4 * b + threadIdx.x];
+        out[threadIdx.x] = v;
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// Side pass 1: ghost-layer cells without a handler. The reference treats them as fluid cells
+// that never stream (domain.hpp:115-141) but collide in place every step (domain.hpp:143-153),
+// each of its two fields on its own: the copy in the field that is collide_field after step t
+// is collided at step t. Interior fluid cells pull from them. Copy (t mod 2) is collided after
+// step t and written into the boundary slots of the neighbours, which pull it at step t + 1.
+// ------------------------------------------------------------------------------------------
+template <class L, class S>
+__global__ void ghost_fluid_kernel(S* pop, const uint8_t* flag, Geom g, double tau,
+                                   const int* gf_xyz, double* gf_pop, int n_gf, int copy)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n_gf) return;
+    double* c = gf_pop + (static_cast<size_t>(copy) * n_gf + j) * L::Q;
+    double f[L::Q];
+#pragma unroll
+    for (int q = 0; q < L::Q; ++q) f[q] = c[q];
+    collide_exact<L>(f, tau);
+    const int x = gf_xyz[3 * j], y = gf_xyz[3 * j + 1], z = gf_xyz[3 * j + 2];
+#pragma unroll
+    for (int q = 0; q < L::Q; ++q) {
+        c[q] = f[q];
+        int nx, ny, nz;
+        nbr_xyz(g, x, y, z, L::c(q, 0), L::c(q, 1), L::c(q, 2), nx, ny, nz);
+        if (!interior(g, nx, ny, nz)) continue;
+        const int n = cidx(g, nx, ny, nz);
+        if (is_fluid(flag[n]))
+            Store<S>::st(pop + static_cast<size_t>(q) * g.PS + n, from_f64<L, S>(f[q], q));
+    }
+}
+
+// Ghost-fluid copies from an AoS FP64 field (lbm_set_populations) and back (get).
+template <class L>
+__global__ void ghost_fluid_io_kernel(Geom g, const int* gf_xyz, double* gf_pop, int n_gf,
+                                      int copy, double* aos, int to_aos)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n_gf) return;
+    double* c = gf_pop + (static_cast<size_t>(copy) * n_gf + j) * L::Q;
+    const size_t r = ref_idx(g, gf_xyz[3 * j], gf_xyz[3 * j + 1], gf_xyz[3 * j + 2]);
+    for (int q = 0; q < L::Q; ++q) {
+        if (to_aos) aos[r * L::Q + q] = c[q];
+        else c[q] = aos[r * L::Q + q];
+    }
+}
+
+// Ghost-fluid copies written into the neighbours' boundary slots (after a scatter).
+template <class L, class S>
+__global__ void ghost_fluid_slots_kernel(S* pop, const uint8_t* flag, Geom g, const int* gf_xyz,
+                                         const double* gf_pop, int n_gf, int copy)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n_gf) return;
+    const double* c = gf_pop + (static_cast<size_t>(copy) * n_gf + j) * L::Q;
+    const int x = gf_xyz[3 * j], y = gf_xyz[3 * j + 1], z = gf_xyz[3 * j + 2];
+    for (int q = 0; q < L::Q; ++q) {
+        int nx, ny, nz;
+        nbr_xyz(g, x, y, z, L::c(q, 0), L::c(q, 1), L::c(q, 2), nx, ny, nz);
+        if (!interior(g, nx, ny, nz)) continue;
+        const int n = cidx(g, nx, ny, nz);
+        if (is_fluid(flag[n]))
+            Store<S>::st(pop + static_cast<size_t>(q) * g.PS + n, from_f64<L, S>(c[q], q));
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// Side pass 2: free-slip links (boundary.hpp:79-115). The handler copies, for each direction q
+// that faces an interior fluid cell, a mirrored post-collision population of another fluid
+// cell; which cell and which direction is fixed by the geometry and precomputed on the host.
+// Link = int4 {dst, q | qs << 8 | kind << 16, src, src_m}: plane q at cell dst receives
+// population qs of source src (kind 0: interior fluid cell whose neighbour along c_qs is src_m;
+// kind 1: ghost-fluid cell number src).
+// ------------------------------------------------------------------------------------------
+template <class L, class S>
+__global__ void free_slip_kernel(S* pop, const uint8_t* flag, Geom g, const int4* links, int n,
+                                 int odd, const double* gf_pop, int n_gf, int copy)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const int4 l = links[j];
+    const int q = l.y & 0xff, qs = (l.y >> 8) & 0xff, kind = (l.y >> 16) & 0xff;
+    typename Store<S>::C v;
+    if (kind == 1) {
+        v = from_f64<L, S>(gf_pop[(static_cast<size_t>(copy) * n_gf + l.z) * L::Q + qs], qs);
+    } else if (!odd && is_fluid(flag[l.w])) {
+        v = Store<S>::ld(pop + static_cast<size_t>(L::Q - 1 - qs) * g.PS + l.z);
+    } else {
+        v = Store<S>::ld(pop + static_cast<size_t>(qs) * g.PS + l.w);
+    }
+    Store<S>::st(pop + static_cast<size_t>(q) * g.PS + l.x, v);
+}
+
+}  // namespace lbmg
