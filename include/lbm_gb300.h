@@ -128,10 +128,11 @@ int lbm_get_stream(lbm_domain* d, void** stream);
 /* Number of completed time steps since creation. */
 int64_t lbm_steps_done(const lbm_domain* d);
 
-/* Device bytes held by the handle, and the algorithmic HBM bytes of one step (2*Q*s per
- * interior fluid cell: one read and one write of every population). */
+/* Device bytes held by the handle, the algorithmic HBM bytes of one step (2*Q*s per interior
+ * fluid cell: one read and one write of every population), the number of interior fluid cells
+ * and the number of kernel launches one step makes. Any pointer may be NULL. */
 int lbm_memory_info(const lbm_domain* d, uint64_t* device_bytes, uint64_t* step_bytes,
-                    uint64_t* fluid_cells);
+                    uint64_t* fluid_cells, uint64_t* launches_per_step);
 
 /* Text of the last error on this handle (or of the last failed lbm_create when d is NULL). */
 const char* lbm_last_error(const lbm_domain* d);

@@ -59,7 +59,7 @@ SIGNATURES = {
     "lbm_get_stream": (ctypes.c_int, [_P, ctypes.POINTER(_P)]),
     "lbm_steps_done": (_I64, [_P]),
     "lbm_memory_info": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64),
-                                       ctypes.POINTER(ctypes.c_uint64)]),
+                                       ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]),
     "lbm_last_error": (ctypes.c_char_p, [_P]),
 }
 

@@ -126,13 +126,15 @@ struct lbm_domain {
     DevBuf<double> gf_pop;
     DevBuf<int4> fs_link;
     DevBuf<double> red;  // 4 * kReduceBlocks partials + 4 totals
+    DevBuf<int> edge;    // layout indices of kFluidEdge cells
+    DevBuf<int> errword; // device error word + edge counter
 
     std::string err;
 
     ~lbm_domain()
     {
         pop.release(); flag.release(); bc.release(); profile.release();
-        gf_xyz.release(); gf_pop.release(); fs_link.release(); red.release();
+        gf_xyz.release(); gf_pop.release(); fs_link.release(); red.release(); edge.release(); errword.release();
         if (stream) cudaStreamDestroy(stream);
     }
 
@@ -170,7 +172,67 @@ struct lbm_domain {
 
     void finalize();
     void build_side_lists();
+    void build_edge_list();
+    void check_device_error();
 };
+
+namespace {
+
+// Appends the layout index of every kFluidEdge cell (order fixed afterwards on the host).
+__global__ void collect_edges_kernel(const uint8_t* flag, Geom g, int* list, int* count, int cap)
+{
+    const int x = 1 + static_cast<int>(blockIdx.x) * kBlockX + static_cast<int>(threadIdx.x);
+    if (x > g.xl) return;
+    const int y = 1 + static_cast<int>(blockIdx.y), z = 1 + static_cast<int>(blockIdx.z);
+    const int i = kXOff + x + g.XS * (y + g.YS * z);
+    if (flag[i] != kFluidEdge) return;
+    const int k = atomicAdd(count, 1);
+    if (k < cap) list[k] = i;
+}
+
+}  // namespace
+
+void lbm_domain::build_edge_list()
+{
+    const Geom& g = dev.g;
+    const dim3 grid(static_cast<unsigned>((g.xl + kBlockX - 1) / kBlockX), static_cast<unsigned>(g.yl),
+                    static_cast<unsigned>(g.zl));
+    int* counter = errword.p + 1;
+    check(cudaMemsetAsync(counter, 0, sizeof(int), stream), "edge count reset");
+    collect_edges_kernel<<<grid, kBlockX, 0, stream>>>(flag.p, g, nullptr, counter, 0);
+    int n = 0;
+    check(cudaMemcpyAsync(&n, counter, sizeof(int), cudaMemcpyDeviceToHost, stream), "edge count");
+    check(cudaStreamSynchronize(stream), "edge count");
+    edge.release();
+    if (n > 0) {
+        edge.alloc(static_cast<size_t>(n), "cudaMalloc(edge list)");
+        check(cudaMemsetAsync(counter, 0, sizeof(int), stream), "edge count reset");
+        collect_edges_kernel<<<grid, kBlockX, 0, stream>>>(flag.p, g, edge.p, counter, n);
+        std::vector<int> h(static_cast<size_t>(n));
+        check(cudaMemcpyAsync(h.data(), edge.p, h.size() * sizeof(int), cudaMemcpyDeviceToHost, stream),
+              "edge list");
+        check(cudaStreamSynchronize(stream), "edge list");
+        std::sort(h.begin(), h.end());  // neighbouring edge cells in neighbouring threads
+        check(cudaMemcpyAsync(edge.p, h.data(), h.size() * sizeof(int), cudaMemcpyHostToDevice, stream),
+              "edge list upload");
+        check(cudaStreamSynchronize(stream), "edge list upload");
+    }
+    dev.edge = edge.p;
+    dev.n_edge = n;
+}
+
+void lbm_domain::check_device_error()
+{
+    int e = 0;
+    check(cudaMemcpyAsync(&e, errword.p, sizeof(int), cudaMemcpyDeviceToHost, stream), "read device error word");
+    check(cudaStreamSynchronize(stream), "read device error word");
+    if (e != 0) {
+        check(cudaMemsetAsync(errword.p, 0, sizeof(int), stream), "clear device error word");
+        check(cudaStreamSynchronize(stream), "clear device error word");
+        throw CudaError("a bounded wait inside the step kernel gave up; the results of the steps since the "
+                        "last check are not valid", LBM_ERR_CUDA);
+    }
+}
 
 // Ghost-fluid cells adjacent to interior fluid (or used as a free-slip source) and the
 // free-slip links, from the host map.
@@ -310,6 +372,7 @@ void lbm_domain::finalize()
     }
     dev.profile = profile.p;
     build_side_lists();
+    build_edge_list();
     fluid_cells = 0;
     for (int z = 1; z <= g.zl; ++z)
         for (int y = 1; y <= g.yl; ++y) {
@@ -370,7 +433,7 @@ int lbm_create(lbm_domain** out, int q, int64_t xl, int64_t yl, int64_t zl, doub
     if (precision < LBM_FP64 || precision > LBM_BF16) { g_create_error = "unknown precision"; return LBM_ERR_ARG; }
     const int64_t XS = (xl + 2 + 31) / 32 * 32, YS = yl + 2, ZS = zl + 2;
     const int64_t cells = XS * YS * ZS;
-    if (xl > (1 << 20) || yl > 65535 || zl > 65535 || cells + 64 >= (int64_t(1) << 31)) {
+    if (xl > (1 << 20) || yl > 65535 || zl > 65535 || cells + 1024 >= (int64_t(1) << 31)) {
         g_create_error = "domain too large (cell index must fit 31 bits, yl and zl <= 65535)";
         return LBM_ERR_ARG;
     }
@@ -388,7 +451,7 @@ int lbm_create(lbm_domain** out, int q, int64_t xl, int64_t yl, int64_t zl, doub
         g.xl = static_cast<int>(xl); g.yl = static_cast<int>(yl); g.zl = static_cast<int>(zl);
         g.XS = static_cast<int>(XS); g.YS = static_cast<int>(YS); g.ZS = static_cast<int>(ZS);
         g.per = 0;
-        g.PS = static_cast<size_t>((cells + 32 + 63) / 64 * 64);
+        g.PS = static_cast<size_t>((cells + 512 + 63) / 64 * 64);
         d->ng = static_cast<size_t>(xl + 2) * (yl + 2) * (zl + 2);
         d->n_interior = static_cast<size_t>(xl) * yl * zl;
         d->dev.q = q;
@@ -405,6 +468,9 @@ int lbm_create(lbm_domain** out, int q, int64_t xl, int64_t yl, int64_t zl, doub
         d->flag.alloc(g.PS, "cudaMalloc(flags)");
         d->bc.alloc(kMaxHandlers, "cudaMalloc(handler table)");
         d->red.alloc(4 * kReduceBlocks + 4, "cudaMalloc(reduction scratch)");
+        d->errword.alloc(2, "cudaMalloc(error word)");
+        check(cudaMemsetAsync(d->errword.p, 0, 2 * sizeof(int), d->stream), "clear error word");
+        d->dev.err = d->errword.p;
         d->dev.pop = d->pop.p;
         d->dev.flag = d->flag.p;
         d->dev.bc = d->bc.p;
@@ -553,6 +619,7 @@ int lbm_get_populations(lbm_domain* d, double* f)
         check(cudaGetLastError(), "gather kernel");
         check(cudaMemcpyAsync(f, tmp.p, tmp.bytes(), cudaMemcpyDeviceToHost, d->stream), "download populations");
         check(cudaStreamSynchronize(d->stream), "get populations");
+        d->check_device_error();
     });
 }
 
@@ -584,6 +651,7 @@ int lbm_moments(lbm_domain* d, double* rho, double* u)
                                   cudaMemcpyDeviceToHost, d->stream),
                   "download velocity");
         check(cudaStreamSynchronize(d->stream), "moments");
+        d->check_device_error();
     });
 }
 
@@ -599,6 +667,7 @@ int lbm_reduce_mass_momentum(lbm_domain* d, double out[4])
         check(cudaGetLastError(), "reduction kernel");
         check(cudaMemcpyAsync(out, total, 4 * sizeof(double), cudaMemcpyDeviceToHost, d->stream), "download totals");
         check(cudaStreamSynchronize(d->stream), "reduction");
+        d->check_device_error();
         for (int k = 0; k < 4; ++k) diverged = diverged || !std::isfinite(out[k]);
         if (diverged) d->err = "non-finite mass or momentum: the run diverged";
     });
@@ -608,7 +677,10 @@ int lbm_reduce_mass_momentum(lbm_domain* d, double out[4])
 
 int lbm_sync(lbm_domain* d)
 {
-    return guarded(d, [&] { check(cudaStreamSynchronize(d->stream), "cudaStreamSynchronize"); });
+    return guarded(d, [&] {
+        check(cudaStreamSynchronize(d->stream), "cudaStreamSynchronize");
+        d->check_device_error();
+    });
 }
 
 int lbm_get_stream(lbm_domain* d, void** stream)
@@ -621,7 +693,8 @@ int lbm_get_stream(lbm_domain* d, void** stream)
 
 int64_t lbm_steps_done(const lbm_domain* d) { return d ? d->steps : -1; }
 
-int lbm_memory_info(const lbm_domain* d, uint64_t* device_bytes, uint64_t* step_bytes, uint64_t* fluid_cells)
+int lbm_memory_info(const lbm_domain* d, uint64_t* device_bytes, uint64_t* step_bytes, uint64_t* fluid_cells,
+                    uint64_t* launches_per_step)
 {
     if (!d) return LBM_ERR_ARG;
     lbm_domain* m = const_cast<lbm_domain*>(d);
@@ -629,9 +702,11 @@ int lbm_memory_info(const lbm_domain* d, uint64_t* device_bytes, uint64_t* step_
         m->finalize();
         if (device_bytes)
             *device_bytes = m->pop.bytes() + m->flag.bytes() + m->bc.bytes() + m->profile.bytes() + m->gf_xyz.bytes() +
-                            m->gf_pop.bytes() + m->fs_link.bytes() + m->red.bytes();
+                            m->gf_pop.bytes() + m->fs_link.bytes() + m->red.bytes() + m->edge.bytes() + m->errword.bytes();
         if (step_bytes) *step_bytes = 2ull * m->Q * store_bytes(m->precision) * m->fluid_cells;
         if (fluid_cells) *fluid_cells = m->fluid_cells;
+        if (launches_per_step)
+            *launches_per_step = 1 + (m->dev.n_edge > 0) + (m->dev.n_gf > 0) + (m->dev.n_fs > 0);
     });
 }
 

@@ -7,6 +7,8 @@
 //           XS = round_up(xl + 2, 32), YS = yl + 2. Interior rows start at column 32, so every
 //           warp's 32 consecutive x cells begin on a 32-element boundary. The ghost cell
 //           x = xl + 1 may spill into the next row's unused columns 0..30.
+//           Planes are PS = round_up(XS*YS*ZS + 512, 64) elements apart; the slack after the
+//           last row absorbs the widened row copies of the row kernel.
 //   flag  : one byte per cell, same indexing (see CellFlag).
 //   State after k steps, in place (AA pattern): for an interior fluid cell x and direction p
 //   with neighbour m = x + c_p,
@@ -68,16 +70,21 @@ struct DomainDev {
     const BcEntry* bc;         // kMaxHandlers entries
     const double* profile;     // 3 doubles per cell in reference cell order, or nullptr
     // Ghost-fluid side pass: cells in the ghost layer without a handler that have at least one
-    // interior fluid neighbour. Two FP64 copies of their populations (the reference's two
-    // fields), gf_cells entries each.
-    const int* gf_cell;        // cell index (layout index) of each ghost-fluid cell
+    // interior fluid neighbour (or feed a free-slip link). Two FP64 copies of their populations
+    // (the reference's two fields), n_gf entries each.
     const int* gf_xyz;         // x, y, z per ghost-fluid cell
     double* gf_pop;            // [2][n_gf][Q]
     int n_gf;
     // Free-slip side pass: one entry per (boundary cell, direction) link that a free-slip
-    // handler writes; see FreeSlipLink.
+    // handler writes (see the free-slip link note below).
     const int4* fs_link;
     int n_fs;
+    // Fluid cells next to a non-fluid cell or a periodic wrap (kFluidEdge), as layout indices in
+    // increasing order: updated by the edge kernel; all other fluid cells by the row kernel.
+    const int* edge;
+    int n_edge;
+    // Device error word: set to 1 by a kernel whose bounded wait gave up.
+    int* err;
 };
 
 // A free-slip link: after a step, plane `q` at fluid cell `dst` receives the post-collision

@@ -9,6 +9,7 @@
 
 #include "domain.cuh"
 #include "lattice.cuh"
+#include "tma.cuh"
 
 namespace lbmg {
 
@@ -291,9 +292,11 @@ __device__ __forceinline__ float bc_value_shifted(const BcEntry& b, int p, const
 }
 
 // ------------------------------------------------------------------------------------------
-// The fused time step: pull-stream + BGK collide + boundary handlers, one thread per interior
-// cell, in place (AA pattern). ODD = the step number (1-based) is odd, i.e. the populations are
-// pulled from the neighbours; even steps read and write the cell's own slots.
+// The fused time step: pull-stream + BGK collide + boundary handlers, in place (AA pattern).
+// ODD = the step number (1-based) is odd: populations are pulled from the neighbours and pushed
+// to them; even steps read and write the cell's own slots. Every cell's read set equals its
+// write set, so cells are independent within a step and the two kernels below (bulk rows and
+// the edge-cell list) may run in either order.
 // ------------------------------------------------------------------------------------------
 template <class S>
 struct StepParams {
@@ -301,71 +304,47 @@ struct StepParams {
     const uint8_t* flag;
     const BcEntry* bc;
     const double* profile;
+    const int* edge;   // layout indices of kFluidEdge cells
+    int n_edge;
+    int* err;          // set to 1 when a bounded wait gives up
     Geom g;
     double tau;
     float omega;
 };
 
+template <class L, class S>
+__device__ __forceinline__ void collide_any(typename Store<S>::C (&f)[L::Q], const StepParams<S>& P)
+{
+    if constexpr (Store<S>::kShifted)
+        collide_shifted<L>(f, P.omega);
+    else
+        collide_exact<L>(f, P.tau);
+}
+
+// General update of one fluid cell next to non-fluid cells or a periodic wrap.
 template <class L, class S, bool ODD>
-__global__ void __launch_bounds__(kBlockX) step_kernel(const StepParams<S> P)
+__device__ __forceinline__ void update_edge_cell(const StepParams<S>& P, int x, int y, int z, int i)
 {
     using St = Store<S>;
     using T = typename St::C;
     constexpr int Q = L::Q;
-    const int x = 1 + static_cast<int>(blockIdx.x) * kBlockX + static_cast<int>(threadIdx.x);
-    if (x > P.g.xl) return;
-    const int y = 1 + static_cast<int>(blockIdx.y);
-    const int z = 1 + static_cast<int>(blockIdx.z);
-    const int i = cidx(P.g, x, y, z);
-    const uint8_t fl = P.flag[i];
-    if (fl > kFluidEdge) return;
-
     S* __restrict__ pop = P.pop;
     const size_t PS = P.g.PS;
-    const int sy = P.g.XS;
-    const int sz = P.g.XS * P.g.YS;
     T f[Q];
-
-    if (fl == kFluidBulk) {
 #pragma unroll
-        for (int q = 0; q < Q; ++q) {
-            const int off = L::c(q, 0) + L::c(q, 1) * sy + L::c(q, 2) * sz;
-            f[q] = ODD ? St::ld(pop + static_cast<size_t>(inv<L>(q)) * PS + (i - off))
-                       : St::ld(pop + static_cast<size_t>(q) * PS + i);
-        }
-    } else {
-#pragma unroll
-        for (int q = 0; q < Q; ++q) {
-            if (ODD) {
-                int nx, ny, nz;
-                nbr_xyz(P.g, x, y, z, -L::c(q, 0), -L::c(q, 1), -L::c(q, 2), nx, ny, nz);
-                const int n = cidx(P.g, nx, ny, nz);
-                f[q] = is_fluid(P.flag[n]) ? St::ld(pop + static_cast<size_t>(inv<L>(q)) * PS + n)
-                                           : St::ld(pop + static_cast<size_t>(q) * PS + i);
-            } else {
-                f[q] = St::ld(pop + static_cast<size_t>(q) * PS + i);
-            }
+    for (int q = 0; q < Q; ++q) {
+        if (ODD) {
+            int nx, ny, nz;
+            nbr_xyz(P.g, x, y, z, -L::c(q, 0), -L::c(q, 1), -L::c(q, 2), nx, ny, nz);
+            const int n = cidx(P.g, nx, ny, nz);
+            f[q] = is_fluid(P.flag[n]) ? St::ld(pop + static_cast<size_t>(inv<L>(q)) * PS + n)
+                                       : St::ld(pop + static_cast<size_t>(q) * PS + i);
+        } else {
+            f[q] = St::ld(pop + static_cast<size_t>(q) * PS + i);
         }
     }
-
-    if constexpr (St::kShifted)
-        collide_shifted<L>(f, P.omega);
-    else
-        collide_exact<L>(f, P.tau);
-
-    if (fl == kFluidBulk) {
-#pragma unroll
-        for (int p = 0; p < Q; ++p) {
-            const int off = L::c(p, 0) + L::c(p, 1) * sy + L::c(p, 2) * sz;
-            if (ODD)
-                St::st(pop + static_cast<size_t>(p) * PS + (i + off), f[p]);
-            else
-                St::st(pop + static_cast<size_t>(inv<L>(p)) * PS + i, f[p]);
-        }
-        return;
-    }
-
-    // Edge cell: moments of the post-collision state for the handlers that need them.
+    collide_any<L, S>(f, P);
+    // moments of the post-collision state for the handlers that need them
     T m0, m1, m2, m3;
     if constexpr (St::kShifted) {
         moments_shifted<L>(f, m0, m1, m2, m3);
@@ -401,6 +380,107 @@ __global__ void __launch_bounds__(kBlockX) step_kernel(const StepParams<S> P)
         else
             val = bc_value_exact<L>(b, p, f, m0, vcell);
         St::st(pop + static_cast<size_t>(inv<L>(p)) * PS + i, val);
+    }
+}
+
+constexpr int kEdgeThreads = 128;
+
+template <class L, class S, bool ODD>
+__global__ void __launch_bounds__(kEdgeThreads) edge_kernel(const StepParams<S> P)
+{
+    const int j = static_cast<int>(blockIdx.x) * kEdgeThreads + static_cast<int>(threadIdx.x);
+    if (j >= P.n_edge) return;
+    const int i = P.edge[j];
+    const int r = i - kXOff;
+    const int x = r % P.g.XS;
+    const int t = r / P.g.XS;
+    update_edge_cell<L, S, ODD>(P, x, t % P.g.YS, t / P.g.YS, i);
+}
+
+// Bulk cells, one block per segment of kRowCells cells of an x-row. One thread brings the Q
+// source rows of the segment into shared memory with bulk asynchronous copies (TMA) on one
+// mbarrier, so the loads in flight are bounded by shared memory rather than registers; every
+// thread then collides its cell from shared memory and stores its Q results. Each copied row is
+// the segment widened by kRowPad elements on both sides (16 bytes), which keeps source and size
+// 16-byte aligned and covers the +-1 shift in x of the odd-step pulls.
+constexpr int kRowCells = 128;
+constexpr uint32_t kMaxPolls = 1u << 22;
+
+template <class S>
+constexpr int row_pad()
+{
+    return static_cast<int>(16 / sizeof(S));
+}
+template <class L, class S>
+constexpr size_t row_smem_bytes()
+{
+    return static_cast<size_t>(L::Q) * (kRowCells + 2 * row_pad<S>()) * sizeof(S);
+}
+
+template <class L, class S, bool ODD>
+__global__ void __launch_bounds__(kRowCells) row_kernel(const StepParams<S> P)
+{
+    using St = Store<S>;
+    using T = typename St::C;
+    constexpr int Q = L::Q;
+    constexpr int PAD = row_pad<S>();
+    constexpr int W = kRowCells + 2 * PAD;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    S* buf = reinterpret_cast<S*>(smem_raw);
+    __shared__ __align__(8) uint64_t bar;
+
+    const int tx = static_cast<int>(threadIdx.x);
+    const int x0 = 1 + static_cast<int>(blockIdx.x) * kRowCells;
+    const int y = 1 + static_cast<int>(blockIdx.y);
+    const int z = 1 + static_cast<int>(blockIdx.z);
+    const int x = x0 + tx;
+    const size_t PS = P.g.PS;
+
+    if (tx == 0) {
+        mbar_init(&bar, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    if (tx == 0) {
+        constexpr uint32_t bytes = W * sizeof(S);
+        mbar_arrive_expect_tx(&bar, Q * bytes);
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            const int plane = ODD ? inv<L>(q) : q;
+            const int ry = ODD ? y - L::c(q, 1) : y;
+            const int rz = ODD ? z - L::c(q, 2) : z;
+            const S* src = P.pop + static_cast<size_t>(plane) * PS +
+                           (static_cast<size_t>(kXOff + x0 - PAD) +
+                            static_cast<size_t>(P.g.XS) * (static_cast<size_t>(ry) + static_cast<size_t>(P.g.YS) * rz));
+            bulk_g2s(buf + q * W, src, bytes, &bar);
+        }
+    }
+    const int i = cidx(P.g, x, y, z);
+    const uint8_t fl = x <= P.g.xl ? P.flag[i] : static_cast<uint8_t>(0xff);
+    if (!mbar_wait_bounded(&bar, 0, kMaxPolls)) {
+        // never leave while copies may still land in this block's shared memory
+        *P.err = 1;
+        mbar_wait_bounded(&bar, 0, kMaxPolls);
+        return;
+    }
+    if (fl != kFluidBulk) return;
+
+    T f[Q];
+#pragma unroll
+    for (int q = 0; q < Q; ++q) f[q] = St::ld(buf + q * W + PAD + tx - (ODD ? L::c(q, 0) : 0));
+    collide_any<L, S>(f, P);
+
+    S* __restrict__ pop = P.pop;
+    const int sy = P.g.XS;
+    const int sz = P.g.XS * P.g.YS;
+#pragma unroll
+    for (int p = 0; p < Q; ++p) {
+        if (ODD) {
+            const int off = L::c(p, 0) + L::c(p, 1) * sy + L::c(p, 2) * sz;
+            St::st(pop + static_cast<size_t>(p) * PS + (i + off), f[p]);
+        } else {
+            St::st(pop + static_cast<size_t>(inv<L>(p)) * PS + i, f[p]);
+        }
     }
 }
 

@@ -29,6 +29,9 @@ StepParams<S> step_params(const DomainDev& d)
     p.bc = d.bc;
     p.profile = d.profile;
     p.g = d.g;
+    p.edge = d.edge;
+    p.n_edge = d.n_edge;
+    p.err = d.err;
     p.tau = d.tau;
     p.omega = static_cast<float>(1.0 / d.tau);
     return p;
@@ -63,10 +66,17 @@ struct Launch {
     static void step(const DomainDev& d, long long t, cudaStream_t s)
     {
         const StepParams<S> p = step_params<S>(d);
-        if (t & 1)
-            step_kernel<L, S, true><<<cell_grid(d.g), kBlockX, 0, s>>>(p);
-        else
-            step_kernel<L, S, false><<<cell_grid(d.g), kBlockX, 0, s>>>(p);
+        const dim3 rows(static_cast<unsigned>((d.g.xl + kRowCells - 1) / kRowCells), static_cast<unsigned>(d.g.yl),
+                        static_cast<unsigned>(d.g.zl));
+        constexpr size_t smem = row_smem_bytes<L, S>();
+        const unsigned eb = static_cast<unsigned>((d.n_edge + kEdgeThreads - 1) / kEdgeThreads);
+        if (t & 1) {
+            row_kernel<L, S, true><<<rows, kRowCells, smem, s>>>(p);
+            if (d.n_edge > 0) edge_kernel<L, S, true><<<eb, kEdgeThreads, 0, s>>>(p);
+        } else {
+            row_kernel<L, S, false><<<rows, kRowCells, smem, s>>>(p);
+            if (d.n_edge > 0) edge_kernel<L, S, false><<<eb, kEdgeThreads, 0, s>>>(p);
+        }
         side_passes(d, t, s);
     }
 

@@ -282,7 +282,8 @@ class Domain:
         return s.value or 0
 
     def memory_info(self):
-        dev, step, fluid = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()
-        check(self._lib.lbm_memory_info(self._h, ctypes.byref(dev), ctypes.byref(step), ctypes.byref(fluid)),
-              self._h)
-        return {"device_bytes": dev.value, "step_bytes": step.value, "fluid_cells": fluid.value}
+        dev, step, fluid, launches = (ctypes.c_uint64() for _ in range(4))
+        check(self._lib.lbm_memory_info(self._h, ctypes.byref(dev), ctypes.byref(step), ctypes.byref(fluid),
+                                        ctypes.byref(launches)), self._h)
+        return {"device_bytes": dev.value, "step_bytes": step.value, "fluid_cells": fluid.value,
+                "launches_per_step": launches.value}
