@@ -126,15 +126,16 @@ struct lbm_domain {
     DevBuf<double> gf_pop;
     DevBuf<int4> fs_link;
     DevBuf<double> red;  // 4 * kReduceBlocks partials + 4 totals
-    DevBuf<int> edge;    // layout indices of kFluidEdge cells
-    DevBuf<int> errword; // device error word + edge counter
+    DevBuf<uint32_t> link;  // per-cell link words
+    DevBuf<int> edge;       // kFluidEdge cells
+    DevBuf<int> errword;    // device error word + a counter
 
     std::string err;
 
     ~lbm_domain()
     {
         pop.release(); flag.release(); bc.release(); profile.release();
-        gf_xyz.release(); gf_pop.release(); fs_link.release(); red.release(); edge.release(); errword.release();
+        gf_xyz.release(); gf_pop.release(); fs_link.release(); red.release(); link.release(); edge.release(); errword.release();
         if (stream) cudaStreamDestroy(stream);
     }
 
@@ -178,7 +179,7 @@ struct lbm_domain {
 
 namespace {
 
-// Appends the layout index of every kFluidEdge cell (order fixed afterwards on the host).
+// Appends the layout index of every kFluidEdge cell (the host sorts the list afterwards).
 __global__ void collect_edges_kernel(const uint8_t* flag, Geom g, int* list, int* count, int cap)
 {
     const int x = 1 + static_cast<int>(blockIdx.x) * kBlockX + static_cast<int>(threadIdx.x);
@@ -195,15 +196,15 @@ __global__ void collect_edges_kernel(const uint8_t* flag, Geom g, int* list, int
 void lbm_domain::build_edge_list()
 {
     const Geom& g = dev.g;
+    edge.release();
     const dim3 grid(static_cast<unsigned>((g.xl + kBlockX - 1) / kBlockX), static_cast<unsigned>(g.yl),
                     static_cast<unsigned>(g.zl));
     int* counter = errword.p + 1;
+    int n = 0;
     check(cudaMemsetAsync(counter, 0, sizeof(int), stream), "edge count reset");
     collect_edges_kernel<<<grid, kBlockX, 0, stream>>>(flag.p, g, nullptr, counter, 0);
-    int n = 0;
     check(cudaMemcpyAsync(&n, counter, sizeof(int), cudaMemcpyDeviceToHost, stream), "edge count");
     check(cudaStreamSynchronize(stream), "edge count");
-    edge.release();
     if (n > 0) {
         edge.alloc(static_cast<size_t>(n), "cudaMalloc(edge list)");
         check(cudaMemsetAsync(counter, 0, sizeof(int), stream), "edge count reset");
@@ -468,6 +469,8 @@ int lbm_create(lbm_domain** out, int q, int64_t xl, int64_t yl, int64_t zl, doub
         d->flag.alloc(g.PS, "cudaMalloc(flags)");
         d->bc.alloc(kMaxHandlers, "cudaMalloc(handler table)");
         d->red.alloc(4 * kReduceBlocks + 4, "cudaMalloc(reduction scratch)");
+        d->link.alloc(g.PS, "cudaMalloc(link words)");
+        d->dev.link = d->link.p;
         d->errword.alloc(2, "cudaMalloc(error word)");
         check(cudaMemsetAsync(d->errword.p, 0, 2 * sizeof(int), d->stream), "clear error word");
         d->dev.err = d->errword.p;
@@ -702,11 +705,11 @@ int lbm_memory_info(const lbm_domain* d, uint64_t* device_bytes, uint64_t* step_
         m->finalize();
         if (device_bytes)
             *device_bytes = m->pop.bytes() + m->flag.bytes() + m->bc.bytes() + m->profile.bytes() + m->gf_xyz.bytes() +
-                            m->gf_pop.bytes() + m->fs_link.bytes() + m->red.bytes() + m->edge.bytes() + m->errword.bytes();
+                            m->gf_pop.bytes() + m->fs_link.bytes() + m->red.bytes() + m->link.bytes() + m->edge.bytes() + m->errword.bytes();
         if (step_bytes) *step_bytes = 2ull * m->Q * store_bytes(m->precision) * m->fluid_cells;
         if (fluid_cells) *fluid_cells = m->fluid_cells;
         if (launches_per_step)
-            *launches_per_step = 1 + (m->dev.n_edge > 0) + (m->dev.n_gf > 0) + (m->dev.n_fs > 0);
+            *launches_per_step = 1 + (m->dev.n_gf > 0) + (m->dev.n_fs > 0);
     });
 }
 

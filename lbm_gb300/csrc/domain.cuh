@@ -10,6 +10,7 @@
 //           Planes are PS = round_up(XS*YS*ZS + 512, 64) elements apart; the slack after the
 //           last row absorbs the widened row copies of the row kernel.
 //   flag  : one byte per cell, same indexing (see CellFlag).
+//   link  : one 32-bit word per cell, same indexing (fluid cells only, see classify_kernel).
 //   State after k steps, in place (AA pattern): for an interior fluid cell x and direction p
 //   with neighbour m = x + c_p,
 //     k even : f*_p(x) is at plane inv(p), cell x when m is fluid; at plane p, cell m otherwise
@@ -79,8 +80,10 @@ struct DomainDev {
     // handler writes (see the free-slip link note below).
     const int4* fs_link;
     int n_fs;
-    // Fluid cells next to a non-fluid cell or a periodic wrap (kFluidEdge), as layout indices in
-    // increasing order: updated by the edge kernel; all other fluid cells by the row kernel.
+    // Per interior fluid cell: which pull neighbours are not fluid (see classify_kernel).
+    uint32_t* link;
+    // kFluidEdge cells as layout indices in increasing order: updated by the edge blocks of the
+    // step kernel; all other fluid cells by its row blocks.
     const int* edge;
     int n_edge;
     // Device error word: set to 1 by a kernel whose bounded wait gave up.

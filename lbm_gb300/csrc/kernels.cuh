@@ -150,14 +150,14 @@ __device__ __forceinline__ double feq_exact(int q, double rho, double u0, double
 {
     double cu = 0.0;
     double uu = 0.0;
-    const int c0 = L::c(q, 0), c1 = L::c(q, 1), c2 = L::c(q, 2);
+    const int c0 = rt_c<L>(q, 0), c1 = rt_c<L>(q, 1), c2 = rt_c<L>(q, 2);
     if (c0 > 0) cu += u0; else if (c0 < 0) cu -= u0;
     uu += u0 * u0;
     if (c1 > 0) cu += u1; else if (c1 < 0) cu -= u1;
     uu += u1 * u1;
     if (c2 > 0) cu += u2; else if (c2 < 0) cu -= u2;
     uu += u2 * u2;
-    return L::w(q) * rho * (1 + cu / kCS2 + (cu) * (cu) / kCS4x2 - uu / kCS2x2);
+    return rt_w<L>(q) * rho * (1 + cu / kCS2 + (cu) * (cu) / kCS4x2 - uu / kCS2x2);
 }
 
 // BGKCollision::collide (collision.hpp:60-70).
@@ -175,23 +175,37 @@ __device__ __forceinline__ void collide_exact(double (&f)[L::Q], double tau)
     }
 }
 
+// Momentum sum_q f_q c_qd of populations kept in memory at fs[q * stride].
+template <class L, class T>
+__device__ __forceinline__ T momentum_mem(const T* fs, int stride, int d)
+{
+    T s = 0;
+#pragma unroll
+    for (int q = 0; q < L::Q; ++q) {
+        const int c = L::c(q, d);
+        if (c > 0) s += fs[q * stride];
+        else if (c < 0) s -= fs[q * stride];
+    }
+    return s;
+}
+
 // Value a boundary cell's handler writes into its direction q = inv(p) for the fluid cell that
-// sees it in direction p, from that fluid cell's post-collision populations fs
-// (boundary.hpp:14-214). rho_s = density_exact(fs).
+// sees it in direction p, from that fluid cell's post-collision populations fs[k * stride]
+// (boundary.hpp:14-214). rho_s = density of fs. p may be known only at run time.
 template <class L>
-__device__ __forceinline__ double bc_value_exact(const BcEntry& b, int p, const double (&fs)[L::Q],
+__device__ __forceinline__ double bc_value_exact(const BcEntry& b, int p, const double* fs, int stride,
                                                  double rho_s, const double* vcell)
 {
     const int q = inv<L>(p);
     switch (b.type) {
     case kMovingWall: {  // boundary.hpp:52-66
         double cu = 0.0;
-        const int c0 = L::c(q, 0), c1 = L::c(q, 1), c2 = L::c(q, 2);
+        const int c0 = rt_c<L>(q, 0), c1 = rt_c<L>(q, 1), c2 = rt_c<L>(q, 2);
         if (c0 > 0) cu += b.v[0]; else if (c0 < 0) cu -= b.v[0];
         if (c1 > 0) cu += b.v[1]; else if (c1 < 0) cu -= b.v[1];
         if (c2 > 0) cu += b.v[2]; else if (c2 < 0) cu -= b.v[2];
-        const double finv = fs[p];
-        return finv + 2.0 * L::w(q) * rho_s * cu / kCS2;
+        const double finv = fs[p * stride];
+        return finv + 2.0 * rt_w<L>(q) * rho_s * cu / kCS2;
     }
     case kInflow: {  // boundary.hpp:173-179
         const double* v = vcell ? vcell : b.v;
@@ -199,13 +213,13 @@ __device__ __forceinline__ double bc_value_exact(const BcEntry& b, int p, const 
     }
     case kOutflow:     // boundary.hpp:137-148
     case kPressure: {  // boundary.hpp:203-212
-        const double u0 = momentum_exact<L>(fs, 0) / b.rho;
-        const double u1 = momentum_exact<L>(fs, 1) / b.rho;
-        const double u2 = momentum_exact<L>(fs, 2) / b.rho;
-        return feq_exact<L>(q, b.rho, u0, u1, u2) + feq_exact<L>(p, b.rho, u0, u1, u2) - fs[p];
+        const double u0 = momentum_mem<L>(fs, stride, 0) / b.rho;
+        const double u1 = momentum_mem<L>(fs, stride, 1) / b.rho;
+        const double u2 = momentum_mem<L>(fs, stride, 2) / b.rho;
+        return feq_exact<L>(q, b.rho, u0, u1, u2) + feq_exact<L>(p, b.rho, u0, u1, u2) - fs[p * stride];
     }
     default:  // kNoSlip, boundary.hpp:22-29
-        return fs[p];
+        return fs[p * stride];
     }
 }
 
@@ -222,8 +236,8 @@ template <class L>
 __device__ __forceinline__ float seq_shifted(int q, float drho, float rho, float ux, float uy,
                                              float uz, float uu_c)
 {
-    const float cu = L::c(q, 0) * ux + L::c(q, 1) * uy + L::c(q, 2) * uz;
-    return static_cast<float>(L::w(q)) * (drho + rho * (cu * (kA + cu * kB) - uu_c));
+    const float cu = rt_c<L>(q, 0) * ux + rt_c<L>(q, 1) * uy + rt_c<L>(q, 2) * uz;
+    return static_cast<float>(rt_w<L>(q)) * (drho + rho * (cu * (kA + cu * kB) - uu_c));
 }
 
 template <class L>
@@ -256,8 +270,10 @@ __device__ __forceinline__ void collide_shifted(float (&s)[L::Q], float omega)
     }
 }
 
+// FP32 counterpart of bc_value_exact on shifted populations ss[k * stride]; drho_s and j are the
+// post-collision moments of the fluid cell.
 template <class L>
-__device__ __forceinline__ float bc_value_shifted(const BcEntry& b, int p, const float (&ss)[L::Q],
+__device__ __forceinline__ float bc_value_shifted(const BcEntry& b, int p, const float* ss, int stride,
                                                   float drho_s, float jx, float jy, float jz,
                                                   const double* vcell)
 {
@@ -265,10 +281,10 @@ __device__ __forceinline__ float bc_value_shifted(const BcEntry& b, int p, const
     switch (b.type) {
     case kMovingWall: {
         const float rho = 1.f + drho_s;
-        const float cu = L::c(q, 0) * static_cast<float>(b.v[0]) +
-                         L::c(q, 1) * static_cast<float>(b.v[1]) +
-                         L::c(q, 2) * static_cast<float>(b.v[2]);
-        return ss[p] + 2.f * static_cast<float>(L::w(q)) * rho * cu * kA;
+        const float cu = rt_c<L>(q, 0) * static_cast<float>(b.v[0]) +
+                         rt_c<L>(q, 1) * static_cast<float>(b.v[1]) +
+                         rt_c<L>(q, 2) * static_cast<float>(b.v[2]);
+        return ss[p * stride] + 2.f * static_cast<float>(rt_w<L>(q)) * rho * cu * kA;
     }
     case kInflow: {
         const double* v = vcell ? vcell : b.v;
@@ -284,10 +300,10 @@ __device__ __forceinline__ float bc_value_shifted(const BcEntry& b, int p, const
         const float ux = jx * ir, uy = jy * ir, uz = jz * ir;
         const float uu_c = (ux * ux + uy * uy + uz * uz) * kC;
         return seq_shifted<L>(q, r - 1.f, r, ux, uy, uz, uu_c) +
-               seq_shifted<L>(p, r - 1.f, r, ux, uy, uz, uu_c) - ss[p];
+               seq_shifted<L>(p, r - 1.f, r, ux, uy, uz, uu_c) - ss[p * stride];
     }
     default:
-        return ss[p];
+        return ss[p * stride];
     }
 }
 
@@ -295,18 +311,18 @@ __device__ __forceinline__ float bc_value_shifted(const BcEntry& b, int p, const
 // The fused time step: pull-stream + BGK collide + boundary handlers, in place (AA pattern).
 // ODD = the step number (1-based) is odd: populations are pulled from the neighbours and pushed
 // to them; even steps read and write the cell's own slots. Every cell's read set equals its
-// write set, so cells are independent within a step and the two kernels below (bulk rows and
-// the edge-cell list) may run in either order.
+// write set, so cells are independent within a step and may be updated in any order.
 // ------------------------------------------------------------------------------------------
 template <class S>
 struct StepParams {
     S* pop;
     const uint8_t* flag;
+    const uint32_t* link;  // per fluid cell: bit q = the pull neighbour x - c_q is not fluid
     const BcEntry* bc;
     const double* profile;
-    const int* edge;   // layout indices of kFluidEdge cells
+    const int* edge;       // layout indices of the kFluidEdge cells, increasing
     int n_edge;
-    int* err;          // set to 1 when a bounded wait gives up
+    int* err;              // set to 1 when a bounded wait gives up
     Geom g;
     double tau;
     float omega;
@@ -321,88 +337,87 @@ __device__ __forceinline__ void collide_any(typename Store<S>::C (&f)[L::Q], con
         collide_exact<L>(f, P.tau);
 }
 
-// General update of one fluid cell next to non-fluid cells or a periodic wrap.
-template <class L, class S, bool ODD>
-__device__ __forceinline__ void update_edge_cell(const StepParams<S>& P, int x, int y, int z, int i)
+// Handler values of an edge cell: for every direction p toward a non-fluid neighbour (bit inv(p)
+// of `link`), the value that neighbour's handler writes for this cell, stored where this cell
+// pulls direction inv(p) next step. fs[k * stride] holds the cell's post-collision populations.
+// Ghost-fluid and free-slip neighbours are skipped: their side passes fill those slots.
+template <class L, class S>
+__device__ __forceinline__ void store_handler_values(const StepParams<S>& P, int x, int y, int z, int i,
+                                                     uint32_t link, const typename Store<S>::C* fs,
+                                                     int stride)
 {
     using St = Store<S>;
     using T = typename St::C;
-    constexpr int Q = L::Q;
-    S* __restrict__ pop = P.pop;
-    const size_t PS = P.g.PS;
-    T f[Q];
-#pragma unroll
-    for (int q = 0; q < Q; ++q) {
-        if (ODD) {
-            int nx, ny, nz;
-            nbr_xyz(P.g, x, y, z, -L::c(q, 0), -L::c(q, 1), -L::c(q, 2), nx, ny, nz);
-            const int n = cidx(P.g, nx, ny, nz);
-            f[q] = is_fluid(P.flag[n]) ? St::ld(pop + static_cast<size_t>(inv<L>(q)) * PS + n)
-                                       : St::ld(pop + static_cast<size_t>(q) * PS + i);
-        } else {
-            f[q] = St::ld(pop + static_cast<size_t>(q) * PS + i);
-        }
-    }
-    collide_any<L, S>(f, P);
-    // moments of the post-collision state for the handlers that need them
-    T m0, m1, m2, m3;
+    T m0, m1, m2, m3;  // post-collision moments for the handlers that need them
     if constexpr (St::kShifted) {
-        moments_shifted<L>(f, m0, m1, m2, m3);
+        m0 = 0.f;
+#pragma unroll
+        for (int q = 0; q < L::Q; ++q) m0 += fs[q * stride];
+        m1 = momentum_mem<L>(fs, stride, 0);
+        m2 = momentum_mem<L>(fs, stride, 1);
+        m3 = momentum_mem<L>(fs, stride, 2);
     } else {
-        m0 = density_exact<L>(f);
+        m0 = 0.0;
+#pragma unroll
+        for (int q = 0; q < L::Q; ++q) m0 += fs[q * stride];
         m1 = m2 = m3 = 0.0;
     }
-#pragma unroll
-    for (int p = 0; p < Q; ++p) {
+    uint32_t bits = link & ((1u << L::Q) - 1u);
+    while (bits) {
+        const int b = __ffs(bits) - 1;
+        bits &= bits - 1u;
+        const int p = inv<L>(b);
         int mx, my, mz;
-        nbr_xyz(P.g, x, y, z, L::c(p, 0), L::c(p, 1), L::c(p, 2), mx, my, mz);
-        const int m = cidx(P.g, mx, my, mz);
-        const uint8_t flm = P.flag[m];
-        if (is_fluid(flm)) {
-            if (ODD)
-                St::st(pop + static_cast<size_t>(p) * PS + m, f[p]);
-            else
-                St::st(pop + static_cast<size_t>(inv<L>(p)) * PS + i, f[p]);
-            continue;
-        }
-        // Not fluid: keep the raw post-collision value in the neighbour's slot (read back by
-        // lbm_get_populations / lbm_moments) and store the handler's value where this cell
-        // pulls direction inv(p) next step.
-        St::st(pop + static_cast<size_t>(p) * PS + m, f[p]);
-        if (flm < kFirstHandler) continue;  // ghost-fluid neighbour: side pass fills the slot
-        const BcEntry& b = P.bc[flm - kFirstHandler];
-        if (b.type == kFreeSlip) continue;  // free-slip side pass fills the slot
+        nbr_xyz(P.g, x, y, z, rt_c<L>(p, 0), rt_c<L>(p, 1), rt_c<L>(p, 2), mx, my, mz);
+        const uint8_t flm = P.flag[cidx(P.g, mx, my, mz)];
+        if (flm < kFirstHandler) continue;
+        const BcEntry& be = P.bc[flm - kFirstHandler];
+        if (be.type == kFreeSlip) continue;
         const double* vcell = nullptr;
-        if (b.type == kInflow && b.has_profile) vcell = P.profile + 3 * ref_idx(P.g, mx, my, mz);
+        if (be.type == kInflow && be.has_profile) vcell = P.profile + 3 * ref_idx(P.g, mx, my, mz);
         T val;
         if constexpr (St::kShifted)
-            val = bc_value_shifted<L>(b, p, f, m0, m1, m2, m3, vcell);
+            val = bc_value_shifted<L>(be, p, fs, stride, m0, m1, m2, m3, vcell);
         else
-            val = bc_value_exact<L>(b, p, f, m0, vcell);
-        St::st(pop + static_cast<size_t>(inv<L>(p)) * PS + i, val);
+            val = bc_value_exact<L>(be, p, fs, stride, m0, vcell);
+        St::st(P.pop + static_cast<size_t>(b) * P.g.PS + i, val);
     }
 }
 
-constexpr int kEdgeThreads = 128;
-
+// Post-collision stores of an edge cell: toward a fluid neighbour the plain AA store; toward a
+// non-fluid neighbour the raw value into that neighbour's slot (read back by
+// lbm_get_populations and lbm_moments). Targets wrap on periodic axes.
 template <class L, class S, bool ODD>
-__global__ void __launch_bounds__(kEdgeThreads) edge_kernel(const StepParams<S> P)
+__device__ __forceinline__ void store_edge_populations(const StepParams<S>& P, int x, int y, int z, int i,
+                                                       uint32_t link, const typename Store<S>::C (&f)[L::Q])
 {
-    const int j = static_cast<int>(blockIdx.x) * kEdgeThreads + static_cast<int>(threadIdx.x);
-    if (j >= P.n_edge) return;
-    const int i = P.edge[j];
-    const int r = i - kXOff;
-    const int x = r % P.g.XS;
-    const int t = r / P.g.XS;
-    update_edge_cell<L, S, ODD>(P, x, t % P.g.YS, t / P.g.YS, i);
+#pragma unroll
+    for (int p = 0; p < L::Q; ++p) {
+        const bool to_boundary = (link >> inv<L>(p)) & 1u;
+        if (ODD || to_boundary) {
+            int mx, my, mz;
+            nbr_xyz(P.g, x, y, z, L::c(p, 0), L::c(p, 1), L::c(p, 2), mx, my, mz);
+            Store<S>::st(P.pop + static_cast<size_t>(p) * P.g.PS + cidx(P.g, mx, my, mz), f[p]);
+        } else {
+            Store<S>::st(P.pop + static_cast<size_t>(inv<L>(p)) * P.g.PS + i, f[p]);
+        }
+    }
 }
 
-// Bulk cells, one block per segment of kRowCells cells of an x-row. One thread brings the Q
-// source rows of the segment into shared memory with bulk asynchronous copies (TMA) on one
-// mbarrier, so the loads in flight are bounded by shared memory rather than registers; every
-// thread then collides its cell from shared memory and stores its Q results. Each copied row is
-// the segment widened by kRowPad elements on both sides (16 bytes), which keeps source and size
-// 16-byte aligned and covers the +-1 shift in x of the odd-step pulls.
+// The step kernel, one launch per time step, with two kinds of blocks.
+//
+// Edge blocks (blockIdx.x < n_edge_blocks) come first, so the block scheduler starts them early
+// and their latency-bound work overlaps the streaming of the row blocks. Each updates up to
+// kRowCells edge cells (fluid cells next to a non-fluid cell or a periodic wrap) from the sorted
+// list P.edge, one per thread, through global memory: pulls from the wrapped neighbours or from
+// the boundary slots, stores through store_edge_populations and store_handler_values (the
+// post-collision populations go through shared memory, where the handler loop reads them).
+//
+// Row blocks update the bulk cells of one segment of kRowCells cells of an x-row, one thread per
+// cell. One thread brings the Q source rows of the segment into shared memory with bulk
+// asynchronous copies (TMA) on one mbarrier, so the loads in flight are bounded by shared memory
+// rather than registers. Each copied row is the segment widened by 16 bytes on both sides, which
+// keeps source and size 16-byte aligned and covers the +-1 shift in x of the odd-step pulls.
 constexpr int kRowCells = 128;
 constexpr uint32_t kMaxPolls = 1u << 22;
 
@@ -414,63 +429,99 @@ constexpr int row_pad()
 template <class L, class S>
 constexpr size_t row_smem_bytes()
 {
-    return static_cast<size_t>(L::Q) * (kRowCells + 2 * row_pad<S>()) * sizeof(S);
+    const size_t rows = static_cast<size_t>(L::Q) * (kRowCells + 2 * row_pad<S>()) * sizeof(S);
+    const size_t scratch = static_cast<size_t>(L::Q) * kRowCells * sizeof(typename Store<S>::C);
+    return rows > scratch ? rows : scratch;
 }
 
 template <class L, class S, bool ODD>
-__global__ void __launch_bounds__(kRowCells) row_kernel(const StepParams<S> P)
+__device__ __forceinline__ void edge_block(const StepParams<S>& P, int blk, unsigned char* smem_raw)
+{
+    using St = Store<S>;
+    using T = typename St::C;
+    constexpr int Q = L::Q;
+    const int tx = static_cast<int>(threadIdx.x);
+    const int j = blk * kRowCells + tx;
+    if (j >= P.n_edge) return;
+    const int i = P.edge[j];
+    const int r = i - kXOff;
+    const int x = r % P.g.XS;
+    const int t = r / P.g.XS;
+    const int y = t % P.g.YS, z = t / P.g.YS;
+    const uint32_t link = P.link[i];
+    S* __restrict__ pop = P.pop;
+    T f[Q];
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        if (!ODD || ((link >> q) & 1u)) {
+            f[q] = St::ld(pop + static_cast<size_t>(q) * P.g.PS + i);
+        } else {
+            int nx, ny, nz;
+            nbr_xyz(P.g, x, y, z, -L::c(q, 0), -L::c(q, 1), -L::c(q, 2), nx, ny, nz);
+            f[q] = St::ld(pop + static_cast<size_t>(inv<L>(q)) * P.g.PS + cidx(P.g, nx, ny, nz));
+        }
+    }
+    collide_any<L, S>(f, P);
+    store_edge_populations<L, S, ODD>(P, x, y, z, i, link, f);
+    if (link & ((1u << Q) - 1u)) {
+        T* fs = reinterpret_cast<T*>(smem_raw) + tx;
+#pragma unroll
+        for (int q = 0; q < Q; ++q) fs[q * kRowCells] = f[q];
+        store_handler_values<L, S>(P, x, y, z, i, link, fs, kRowCells);
+    }
+}
+
+template <class L, class S, bool ODD>
+__device__ __forceinline__ void row_block(const StepParams<S>& P, int seg, int nseg_x, unsigned char* smem_raw,
+                                          uint64_t* bar)
 {
     using St = Store<S>;
     using T = typename St::C;
     constexpr int Q = L::Q;
     constexpr int PAD = row_pad<S>();
     constexpr int W = kRowCells + 2 * PAD;
-    extern __shared__ __align__(128) unsigned char smem_raw[];
     S* buf = reinterpret_cast<S*>(smem_raw);
-    __shared__ __align__(8) uint64_t bar;
-
     const int tx = static_cast<int>(threadIdx.x);
-    const int x0 = 1 + static_cast<int>(blockIdx.x) * kRowCells;
-    const int y = 1 + static_cast<int>(blockIdx.y);
-    const int z = 1 + static_cast<int>(blockIdx.z);
+    const int x0 = 1 + (seg % nseg_x) * kRowCells;
+    const int yz = seg / nseg_x;
+    const int y = 1 + yz % P.g.yl;
+    const int z = 1 + yz / P.g.yl;
     const int x = x0 + tx;
     const size_t PS = P.g.PS;
+    S* __restrict__ pop = P.pop;
 
     if (tx == 0) {
-        mbar_init(&bar, 1);
+        mbar_init(bar, 1);
         fence_mbar_init();
     }
     __syncthreads();
     if (tx == 0) {
         constexpr uint32_t bytes = W * sizeof(S);
-        mbar_arrive_expect_tx(&bar, Q * bytes);
+        mbar_arrive_expect_tx(bar, Q * bytes);
 #pragma unroll
         for (int q = 0; q < Q; ++q) {
+            // bulk cells never pull across a periodic wrap, so no source row needs wrapping
             const int plane = ODD ? inv<L>(q) : q;
             const int ry = ODD ? y - L::c(q, 1) : y;
             const int rz = ODD ? z - L::c(q, 2) : z;
-            const S* src = P.pop + static_cast<size_t>(plane) * PS +
+            const S* src = pop + static_cast<size_t>(plane) * PS +
                            (static_cast<size_t>(kXOff + x0 - PAD) +
                             static_cast<size_t>(P.g.XS) * (static_cast<size_t>(ry) + static_cast<size_t>(P.g.YS) * rz));
-            bulk_g2s(buf + q * W, src, bytes, &bar);
+            bulk_g2s(buf + q * W, src, bytes, bar);
         }
     }
     const int i = cidx(P.g, x, y, z);
-    const uint8_t fl = x <= P.g.xl ? P.flag[i] : static_cast<uint8_t>(0xff);
-    if (!mbar_wait_bounded(&bar, 0, kMaxPolls)) {
-        // never leave while copies may still land in this block's shared memory
-        *P.err = 1;
-        mbar_wait_bounded(&bar, 0, kMaxPolls);
+    const bool bulk = x <= P.g.xl && P.flag[i] == kFluidBulk;
+    if (!mbar_wait_bounded(bar, 0, kMaxPolls)) {
+        *P.err = 1;  // never leave while copies may still land in this block's shared memory
+        mbar_wait_bounded(bar, 0, kMaxPolls);
         return;
     }
-    if (fl != kFluidBulk) return;
-
+    if (!bulk) return;
     T f[Q];
 #pragma unroll
     for (int q = 0; q < Q; ++q) f[q] = St::ld(buf + q * W + PAD + tx - (ODD ? L::c(q, 0) : 0));
     collide_any<L, S>(f, P);
-
-    S* __restrict__ pop = P.pop;
     const int sy = P.g.XS;
     const int sz = P.g.XS * P.g.YS;
 #pragma unroll
@@ -482,6 +533,18 @@ __global__ void __launch_bounds__(kRowCells) row_kernel(const StepParams<S> P)
             St::st(pop + static_cast<size_t>(inv<L>(p)) * PS + i, f[p]);
         }
     }
+}
+
+template <class L, class S, bool ODD>
+__global__ void __launch_bounds__(kRowCells) step_kernel(const StepParams<S> P, int n_edge_blocks, int nseg_x)
+{
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ __align__(8) uint64_t bar;
+    const int b = static_cast<int>(blockIdx.x);
+    if (b < n_edge_blocks)
+        edge_block<L, S, ODD>(P, b, smem_raw);
+    else
+        row_block<L, S, ODD>(P, b - n_edge_blocks, nseg_x, smem_raw, &bar);
 }
 
 // ------------------------------------------------------------------------------------------

@@ -107,4 +107,53 @@ __host__ __device__ constexpr int inv(int q)
     return L::Q - 1 - q;
 }
 
+// Velocity components and weights for a direction index known only at run time, without a
+// table in memory: each component is packed as 2 bits (c + 1) into compile-time constants, and
+// each weight as a 2-bit class (one of at most four distinct weights).
+template <class L>
+struct Packed {
+    static constexpr uint64_t bits(int lo, int hi)
+    {
+        uint64_t v = 0;
+        for (int k = lo; k < hi && k < 3 * L::Q; ++k)
+            v |= static_cast<uint64_t>(L::c(k / 3, k % 3) + 1) << (2 * (k - lo));
+        return v;
+    }
+    static constexpr uint64_t kC0 = bits(0, 32);   // components 0..31
+    static constexpr uint64_t kC1 = bits(32, 64);  // components 32..63
+    static constexpr uint64_t kC2 = bits(64, 96);  // components 64..80
+    // representative direction of each weight class (at most four distinct weights)
+    static constexpr int kRep0 = 0;
+    static constexpr int kRep1 = L::Q == 15 ? 2 : (L::Q == 19 ? 2 : 1);
+    static constexpr int kRep2 = L::Q == 15 ? 7 : (L::Q == 19 ? 9 : 4);
+    static constexpr int kRep3 = L::Q == 27 ? 13 : kRep2;
+    static constexpr int wclass(double w)
+    {
+        return w == L::w(kRep0) ? 0 : (w == L::w(kRep1) ? 1 : (w == L::w(kRep2) ? 2 : 3));
+    }
+    static constexpr uint64_t wbits()
+    {
+        uint64_t v = 0;
+        for (int q = 0; q < L::Q; ++q) v |= static_cast<uint64_t>(wclass(L::w(q))) << (2 * q);
+        return v;
+    }
+    static constexpr uint64_t kWC = wbits();
+};
+
+template <class L>
+__host__ __device__ __forceinline__ int rt_c(int q, int d)
+{
+    const int k = 3 * q + d;
+    const uint64_t word = k < 32 ? Packed<L>::kC0 : (k < 64 ? Packed<L>::kC1 : Packed<L>::kC2);
+    return static_cast<int>((word >> (2 * (k & 31))) & 3u) - 1;
+}
+
+template <class L>
+__host__ __device__ __forceinline__ double rt_w(int q)
+{
+    const int cls = static_cast<int>((Packed<L>::kWC >> (2 * q)) & 3u);
+    return cls == 0 ? L::w(Packed<L>::kRep0)
+                    : (cls == 1 ? L::w(Packed<L>::kRep1) : (cls == 2 ? L::w(Packed<L>::kRep2) : L::w(Packed<L>::kRep3)));
+}
+
 }  // namespace lbmg

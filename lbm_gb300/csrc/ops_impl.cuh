@@ -26,11 +26,12 @@ StepParams<S> step_params(const DomainDev& d)
     StepParams<S> p;
     p.pop = static_cast<S*>(d.pop);
     p.flag = d.flag;
+    p.link = d.link;
     p.bc = d.bc;
-    p.profile = d.profile;
-    p.g = d.g;
     p.edge = d.edge;
     p.n_edge = d.n_edge;
+    p.profile = d.profile;
+    p.g = d.g;
     p.err = d.err;
     p.tau = d.tau;
     p.omega = static_cast<float>(1.0 / d.tau);
@@ -48,7 +49,7 @@ struct Launch {
 
     static void classify(const DomainDev& d, cudaStream_t s)
     {
-        classify_kernel<L><<<cell_grid(d.g), kBlockX, 0, s>>>(d.flag, d.g);
+        classify_kernel<L><<<cell_grid(d.g), kBlockX, 0, s>>>(d.flag, d.link, d.g);
     }
 
     static void side_passes(const DomainDev& d, long long k, cudaStream_t s)
@@ -66,17 +67,16 @@ struct Launch {
     static void step(const DomainDev& d, long long t, cudaStream_t s)
     {
         const StepParams<S> p = step_params<S>(d);
-        const dim3 rows(static_cast<unsigned>((d.g.xl + kRowCells - 1) / kRowCells), static_cast<unsigned>(d.g.yl),
-                        static_cast<unsigned>(d.g.zl));
+        const int nseg_x = (d.g.xl + kRowCells - 1) / kRowCells;
+        const long long nseg = static_cast<long long>(nseg_x) * d.g.yl * d.g.zl;
+        const int n_edge_blocks = (d.n_edge + kRowCells - 1) / kRowCells;
+        const unsigned blocks = static_cast<unsigned>(n_edge_blocks + nseg);
         constexpr size_t smem = row_smem_bytes<L, S>();
-        const unsigned eb = static_cast<unsigned>((d.n_edge + kEdgeThreads - 1) / kEdgeThreads);
-        if (t & 1) {
-            row_kernel<L, S, true><<<rows, kRowCells, smem, s>>>(p);
-            if (d.n_edge > 0) edge_kernel<L, S, true><<<eb, kEdgeThreads, 0, s>>>(p);
-        } else {
-            row_kernel<L, S, false><<<rows, kRowCells, smem, s>>>(p);
-            if (d.n_edge > 0) edge_kernel<L, S, false><<<eb, kEdgeThreads, 0, s>>>(p);
-        }
+        static_assert(smem <= 48 * 1024, "step kernel shared memory above the default limit");
+        if (t & 1)
+            step_kernel<L, S, true><<<blocks, kRowCells, smem, s>>>(p, n_edge_blocks, nseg_x);
+        else
+            step_kernel<L, S, false><<<blocks, kRowCells, smem, s>>>(p, n_edge_blocks, nseg_x);
         side_passes(d, t, s);
     }
 

@@ -21,10 +21,10 @@ __global__ void init_kernel(S* pop, size_t PS)
 }
 
 // Interior fluid cells: kFluidEdge when some neighbour is not fluid or lies across a periodic
-// wrap, else kFluidBulk. The lattice is symmetric, so checking x + c_q for all q covers both the
-// pull (x - c_q) and the push (x + c_q) neighbours.
+// wrap, else kFluidBulk; and their link word (bit q: the pull neighbour x - c_q is not fluid).
+// The lattice is symmetric, so the pull neighbours x - c_q are also all the push neighbours.
 template <class L>
-__global__ void classify_kernel(uint8_t* flag, Geom g)
+__global__ void classify_kernel(uint8_t* flag, uint32_t* link, Geom g)
 {
     const int x = 1 + static_cast<int>(blockIdx.x) * kBlockX + static_cast<int>(threadIdx.x);
     if (x > g.xl) return;
@@ -32,17 +32,22 @@ __global__ void classify_kernel(uint8_t* flag, Geom g)
     const int i = cidx(g, x, y, z);
     if (!is_fluid(flag[i])) return;
     bool edge = false;
+    uint32_t m = 0;
 #pragma unroll
     for (int q = 0; q < L::Q; ++q) {
-        const int ax = x + L::c(q, 0), ay = y + L::c(q, 1), az = z + L::c(q, 2);
+        const int ax = x - L::c(q, 0), ay = y - L::c(q, 1), az = z - L::c(q, 2);
         int nx, ny, nz;
-        nbr_xyz(g, x, y, z, L::c(q, 0), L::c(q, 1), L::c(q, 2), nx, ny, nz);
+        nbr_xyz(g, x, y, z, -L::c(q, 0), -L::c(q, 1), -L::c(q, 2), nx, ny, nz);
         if (nx != ax || ny != ay || nz != az) edge = true;
         // flags of fluid cells only move between kFluidBulk and kFluidEdge here, so this read
         // of a neighbour's flag sees the same fluid / non-fluid answer whatever the timing
-        if (!is_fluid(flag[cidx(g, nx, ny, nz)])) edge = true;
+        if (!is_fluid(flag[cidx(g, nx, ny, nz)])) {
+            edge = true;
+            m |= 1u << q;
+        }
     }
     flag[i] = edge ? kFluidEdge : kFluidBulk;
+    link[i] = m;
 }
 
 // Device layout -> AoS FP64 field over all cells (reference cell order).
