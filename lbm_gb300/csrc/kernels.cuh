@@ -260,7 +260,7 @@ __device__ __forceinline__ void collide_shifted(float (&s)[L::Q], float omega)
     float drho, jx, jy, jz;
     moments_shifted<L>(s, drho, jx, jy, jz);
     const float rho = 1.f + drho;
-    const float ir = 1.f / rho;
+    const float ir = __frcp_rn(rho);
     const float ux = jx * ir, uy = jy * ir, uz = jz * ir;
     const float uu_c = (ux * ux + uy * uy + uz * uz) * kC;
 #pragma unroll
@@ -406,8 +406,8 @@ __device__ __forceinline__ void store_edge_populations(const StepParams<S>& P, i
 
 // The step kernel, one launch per time step, with two kinds of blocks.
 //
-// Edge blocks (blockIdx.x < n_edge_blocks) come first, so the block scheduler starts them early
-// and their latency-bound work overlaps the streaming of the row blocks. Each updates up to
+// Edge blocks are interleaved with the row blocks (see step_kernel), so that their
+// latency-bound work overlaps the streaming of the row blocks. Each updates up to
 // kRowCells edge cells (fluid cells next to a non-fluid cell or a periodic wrap) from the sorted
 // list P.edge, one per thread, through global memory: pulls from the wrapped neighbours or from
 // the boundary slots, stores through store_edge_populations and store_handler_values (the
@@ -535,14 +535,21 @@ __device__ __forceinline__ void row_block(const StepParams<S>& P, int seg, int n
     }
 }
 
+// Edge blocks sit at every `edge_stride`-th block index (the first n_edge_blocks such
+// positions), so that the latency-bound edge work is spread over the whole launch instead of
+// holding the SMs at its start; the row blocks fill the other indices in order.
 template <class L, class S, bool ODD>
-__global__ void __launch_bounds__(kRowCells) step_kernel(const StepParams<S> P, int n_edge_blocks, int nseg_x)
+__global__ void __launch_bounds__(kRowCells)
+    step_kernel(const StepParams<S> P, int n_edge_blocks, int edge_stride, int nseg_x)
 {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ __align__(8) uint64_t bar;
     const int b = static_cast<int>(blockIdx.x);
-    if (b < n_edge_blocks)
-        edge_block<L, S, ODD>(P, b, smem_raw);
+    const int interleaved = n_edge_blocks * edge_stride;
+    if (b < interleaved && b % edge_stride == 0)
+        edge_block<L, S, ODD>(P, b / edge_stride, smem_raw);
+    else if (b < interleaved)
+        row_block<L, S, ODD>(P, b - (b / edge_stride + 1), nseg_x, smem_raw, &bar);
     else
         row_block<L, S, ODD>(P, b - n_edge_blocks, nseg_x, smem_raw, &bar);
 }

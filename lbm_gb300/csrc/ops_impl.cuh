@@ -70,13 +70,15 @@ struct Launch {
         const int nseg_x = (d.g.xl + kRowCells - 1) / kRowCells;
         const long long nseg = static_cast<long long>(nseg_x) * d.g.yl * d.g.zl;
         const int n_edge_blocks = (d.n_edge + kRowCells - 1) / kRowCells;
-        const unsigned blocks = static_cast<unsigned>(n_edge_blocks + nseg);
+        const long long total = n_edge_blocks + nseg;
+        const int edge_stride = n_edge_blocks > 0 ? static_cast<int>(total / n_edge_blocks) : 1;
+        const unsigned blocks = static_cast<unsigned>(total);
         constexpr size_t smem = row_smem_bytes<L, S>();
         static_assert(smem <= 48 * 1024, "step kernel shared memory above the default limit");
         if (t & 1)
-            step_kernel<L, S, true><<<blocks, kRowCells, smem, s>>>(p, n_edge_blocks, nseg_x);
+            step_kernel<L, S, true><<<blocks, kRowCells, smem, s>>>(p, n_edge_blocks, edge_stride, nseg_x);
         else
-            step_kernel<L, S, false><<<blocks, kRowCells, smem, s>>>(p, n_edge_blocks, nseg_x);
+            step_kernel<L, S, false><<<blocks, kRowCells, smem, s>>>(p, n_edge_blocks, edge_stride, nseg_x);
         side_passes(d, t, s);
     }
 
