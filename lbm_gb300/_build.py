@@ -45,9 +45,9 @@ def _deps() -> list[Path]:
     return sorted(CSRC.glob("*.cuh")) + [INCLUDE / "lbm_gb300.h"]
 
 
-def _compile(name: str, extra: list[str], verbose: bool) -> Path:
+def _compile(name: str, extra: list[str], verbose: bool, objdir: Path = OBJDIR) -> Path:
     src = CSRC / f"{name}.cu"
-    obj = OBJDIR / f"{name}.o"
+    obj = objdir / f"{name}.o"
     newest = max(p.stat().st_mtime for p in _deps() + [src])
     if obj.exists() and obj.stat().st_mtime >= newest:
         return obj
@@ -62,17 +62,21 @@ def _compile(name: str, extra: list[str], verbose: bool) -> Path:
     return obj
 
 
-def build(verbose: bool = False) -> Path:
-    """Compile every translation unit (in parallel) and link liblbm_gb300.so; returns its path."""
-    OBJDIR.mkdir(parents=True, exist_ok=True)
+def build(verbose: bool = False, out_dir: Path | None = None, defines: tuple = ()) -> Path:
+    """Compile every translation unit (in parallel) and link liblbm_gb300.so; returns its path.
+    out_dir / defines build a separately configured copy (e.g. a different block size) elsewhere."""
+    objdir = OBJDIR if out_dir is None else Path(out_dir) / "obj"
+    lib = LIB if out_dir is None else Path(out_dir) / "liblbm_gb300.so"
+    objdir.mkdir(parents=True, exist_ok=True)
+    flags = [f"-D{d}" for d in defines]
     with ThreadPoolExecutor(max_workers=len(UNITS)) as pool:
-        objs = list(pool.map(lambda kv: _compile(kv[0], kv[1], verbose), UNITS.items()))
-    if not LIB.exists() or LIB.stat().st_mtime < max(o.stat().st_mtime for o in objs):
-        cmd = [nvcc(), *ARCH, "-shared", "-o", str(LIB), *map(str, objs)]
+        objs = list(pool.map(lambda kv: _compile(kv[0], kv[1] + flags, verbose, objdir), UNITS.items()))
+    if not lib.exists() or lib.stat().st_mtime < max(o.stat().st_mtime for o in objs):
+        cmd = [nvcc(), *ARCH, "-shared", "-o", str(lib), *map(str, objs)]
         res = subprocess.run(cmd, capture_output=True, text=True)
         if res.returncode != 0:
             raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")
-    return LIB
+    return lib
 
 
 if __name__ == "__main__":

@@ -6,6 +6,7 @@ missing: there is no CPU fallback for any entry point.
 from __future__ import annotations
 
 import ctypes
+import os
 from pathlib import Path
 
 from . import _build
@@ -76,7 +77,9 @@ _lib = None
 
 
 def library_path() -> Path:
-    return _build.LIB
+    """liblbm_gb300.so in the package, or the file named by $LBM_GB300_LIBRARY."""
+    env = os.environ.get("LBM_GB300_LIBRARY")
+    return Path(env) if env else _build.LIB
 
 
 def load_library(build_if_missing: bool = False) -> ctypes.CDLL:

@@ -254,6 +254,9 @@ __device__ __forceinline__ void moments_shifted(const float (&s)[L::Q], float& d
     }
 }
 
+// BGK on shifted populations. Per opposite pair (q, inv q) the equilibria share
+// sym = drho - rho uu/(2 cs2) + rho cu^2/(2 cs4) and differ in the sign of asym = rho cu/cs2:
+//   s_eq,q - ... = w_q (sym +- asym),   s_q <- s_q + omega (w_q (sym +- asym) - s_q).
 template <class L>
 __device__ __forceinline__ void collide_shifted(float (&s)[L::Q], float omega)
 {
@@ -262,11 +265,18 @@ __device__ __forceinline__ void collide_shifted(float (&s)[L::Q], float omega)
     const float rho = 1.f + drho;
     const float ir = __frcp_rn(rho);
     const float ux = jx * ir, uy = jy * ir, uz = jz * ir;
-    const float uu_c = (ux * ux + uy * uy + uz * uz) * kC;
+    const float base = fmaf(-rho * kC, ux * ux + uy * uy + uz * uz, drho);
+    const float rA = rho * kA, rB = rho * kB;
+    constexpr int R = L::REST;
+    s[R] = fmaf(omega, fmaf(static_cast<float>(L::w(R)), base, -s[R]), s[R]);
 #pragma unroll
-    for (int q = 0; q < L::Q; ++q) {
-        const float seq = seq_shifted<L>(q, drho, rho, ux, uy, uz, uu_c);
-        s[q] = fmaf(omega, seq - s[q], s[q]);
+    for (int q = 0; q < R; ++q) {
+        const float cu = L::c(q, 0) * ux + L::c(q, 1) * uy + L::c(q, 2) * uz;
+        const float sym = fmaf(cu * cu, rB, base);
+        const float asym = cu * rA;
+        const float w = static_cast<float>(L::w(q));
+        s[q] = fmaf(omega, fmaf(w, sym + asym, -s[q]), s[q]);
+        s[L::Q - 1 - q] = fmaf(omega, fmaf(w, sym - asym, -s[L::Q - 1 - q]), s[L::Q - 1 - q]);
     }
 }
 
@@ -413,25 +423,45 @@ __device__ __forceinline__ void store_edge_populations(const StepParams<S>& P, i
 // the boundary slots, stores through store_edge_populations and store_handler_values (the
 // post-collision populations go through shared memory, where the handler loop reads them).
 //
-// Row blocks update the bulk cells of one segment of kRowCells cells of an x-row, one thread per
-// cell. One thread brings the Q source rows of the segment into shared memory with bulk
-// asynchronous copies (TMA) on one mbarrier, so the loads in flight are bounded by shared memory
-// rather than registers. Each copied row is the segment widened by 16 bytes on both sides, which
-// keeps source and size 16-byte aligned and covers the +-1 shift in x of the odd-step pulls.
-constexpr int kRowCells = 128;
-constexpr uint32_t kMaxPolls = 1u << 22;
+// Row blocks update the bulk cells of kSegs consecutive segments of kRowCells cells of x-rows,
+// one thread per cell. At the start the first warp brings the Q source rows of every segment into
+// its own shared-memory stage with bulk asynchronous copies (TMA), one copy per lane, each stage
+// completing on its own mbarrier; the block then collides the segments in order, the later
+// copies landing while the earlier segments compute. The loads in flight are bounded by shared
+// memory rather than registers. Each copied row is the segment widened by 16 bytes on both
+// sides, which keeps source and size 16-byte aligned and covers the +-1 shift in x of the
+// odd-step pulls.
+#ifndef LBMG_ROW_CELLS
+#define LBMG_ROW_CELLS 128
+#endif
+#ifndef LBMG_SEGS
+#define LBMG_SEGS 1
+#endif
+#ifndef LBMG_MIN_BLOCKS
+#define LBMG_MIN_BLOCKS 1
+#endif
+constexpr int kRowCells = LBMG_ROW_CELLS;
+constexpr int kSegs = LBMG_SEGS;
+constexpr uint32_t kMaxPolls = 1u << 20;
 
 template <class S>
 constexpr int row_pad()
 {
     return static_cast<int>(16 / sizeof(S));
 }
+// one stage: the widened rows of a segment, or (edge blocks) the handler scratch
 template <class L, class S>
-constexpr size_t row_smem_bytes()
+constexpr size_t stage_bytes()
 {
     const size_t rows = static_cast<size_t>(L::Q) * (kRowCells + 2 * row_pad<S>()) * sizeof(S);
     const size_t scratch = static_cast<size_t>(L::Q) * kRowCells * sizeof(typename Store<S>::C);
-    return rows > scratch ? rows : scratch;
+    const size_t m = rows > scratch ? rows : scratch;
+    return (m + 127) / 128 * 128;
+}
+template <class L, class S>
+constexpr size_t row_smem_bytes()
+{
+    return kSegs * stage_bytes<L, S>();
 }
 
 template <class L, class S, bool ODD>
@@ -471,66 +501,85 @@ __device__ __forceinline__ void edge_block(const StepParams<S>& P, int blk, unsi
     }
 }
 
+__device__ __forceinline__ void segment_origin(const Geom& g, int seg, int nseg_x, int& x0, int& y, int& z)
+{
+    x0 = 1 + (seg % nseg_x) * kRowCells;
+    const int yz = seg / nseg_x;
+    y = 1 + yz % g.yl;
+    z = 1 + yz / g.yl;
+}
+
 template <class L, class S, bool ODD>
-__device__ __forceinline__ void row_block(const StepParams<S>& P, int seg, int nseg_x, unsigned char* smem_raw,
-                                          uint64_t* bar)
+__device__ __forceinline__ void row_block(const StepParams<S>& P, int rb, int nseg, int nseg_x,
+                                          unsigned char* smem_raw, uint64_t* bars)
 {
     using St = Store<S>;
     using T = typename St::C;
     constexpr int Q = L::Q;
     constexpr int PAD = row_pad<S>();
     constexpr int W = kRowCells + 2 * PAD;
-    S* buf = reinterpret_cast<S*>(smem_raw);
+    constexpr size_t SB = stage_bytes<L, S>();
+    constexpr uint32_t bytes = W * sizeof(S);
     const int tx = static_cast<int>(threadIdx.x);
-    const int x0 = 1 + (seg % nseg_x) * kRowCells;
-    const int yz = seg / nseg_x;
-    const int y = 1 + yz % P.g.yl;
-    const int z = 1 + yz / P.g.yl;
-    const int x = x0 + tx;
     const size_t PS = P.g.PS;
     S* __restrict__ pop = P.pop;
+    const int seg0 = rb * kSegs;
+    const int nsegs = nseg - seg0 < kSegs ? nseg - seg0 : kSegs;
 
     if (tx == 0) {
-        mbar_init(bar, 1);
+#pragma unroll
+        for (int s = 0; s < kSegs; ++s) mbar_init(&bars[s], 1);
         fence_mbar_init();
     }
     __syncthreads();
-    if (tx == 0) {
-        constexpr uint32_t bytes = W * sizeof(S);
-        mbar_arrive_expect_tx(bar, Q * bytes);
-#pragma unroll
-        for (int q = 0; q < Q; ++q) {
-            // bulk cells never pull across a periodic wrap, so no source row needs wrapping
-            const int plane = ODD ? inv<L>(q) : q;
-            const int ry = ODD ? y - L::c(q, 1) : y;
-            const int rz = ODD ? z - L::c(q, 2) : z;
-            const S* src = pop + static_cast<size_t>(plane) * PS +
-                           (static_cast<size_t>(kXOff + x0 - PAD) +
-                            static_cast<size_t>(P.g.XS) * (static_cast<size_t>(ry) + static_cast<size_t>(P.g.YS) * rz));
-            bulk_g2s(buf + q * W, src, bytes, bar);
+    if (tx < 32) {
+        const int lane = tx;
+        for (int s = 0; s < nsegs; ++s) {
+            int x0, y, z;
+            segment_origin(P.g, seg0 + s, nseg_x, x0, y, z);
+            if (lane == 0) mbar_arrive_expect_tx(&bars[s], Q * bytes);
+            __syncwarp();
+            if (lane < Q) {
+                // bulk cells never pull across a periodic wrap, so no source row needs wrapping
+                const int q = lane;
+                const int plane = ODD ? inv<L>(q) : q;
+                const int ry = ODD ? y - rt_c<L>(q, 1) : y;
+                const int rz = ODD ? z - rt_c<L>(q, 2) : z;
+                const S* src = pop + static_cast<size_t>(plane) * PS +
+                               (static_cast<size_t>(kXOff + x0 - PAD) +
+                                static_cast<size_t>(P.g.XS) * (static_cast<size_t>(ry) + static_cast<size_t>(P.g.YS) * rz));
+                bulk_g2s(reinterpret_cast<S*>(smem_raw + s * SB) + q * W, src, bytes, &bars[s]);
+            }
         }
     }
-    const int i = cidx(P.g, x, y, z);
-    const bool bulk = x <= P.g.xl && P.flag[i] == kFluidBulk;
-    if (!mbar_wait_bounded(bar, 0, kMaxPolls)) {
-        *P.err = 1;  // never leave while copies may still land in this block's shared memory
-        mbar_wait_bounded(bar, 0, kMaxPolls);
-        return;
-    }
-    if (!bulk) return;
-    T f[Q];
-#pragma unroll
-    for (int q = 0; q < Q; ++q) f[q] = St::ld(buf + q * W + PAD + tx - (ODD ? L::c(q, 0) : 0));
-    collide_any<L, S>(f, P);
     const int sy = P.g.XS;
     const int sz = P.g.XS * P.g.YS;
+    for (int s = 0; s < nsegs; ++s) {
+        int x0, y, z;
+        segment_origin(P.g, seg0 + s, nseg_x, x0, y, z);
+        const int x = x0 + tx;
+        const int i = cidx(P.g, x, y, z);
+        const bool bulk = x <= P.g.xl && P.flag[i] == kFluidBulk;
+        if (!mbar_wait_bounded(&bars[s], 0, kMaxPolls)) {
+            *P.err = 1;
+            // never leave while copies may still land in this block's shared memory
+            for (int r = s; r < nsegs; ++r) mbar_wait_bounded(&bars[r], 0, kMaxPolls);
+            return;
+        }
+        if (!bulk) continue;
+        const S* buf = reinterpret_cast<const S*>(smem_raw + s * SB);
+        T f[Q];
 #pragma unroll
-    for (int p = 0; p < Q; ++p) {
-        if (ODD) {
-            const int off = L::c(p, 0) + L::c(p, 1) * sy + L::c(p, 2) * sz;
-            St::st(pop + static_cast<size_t>(p) * PS + (i + off), f[p]);
-        } else {
-            St::st(pop + static_cast<size_t>(inv<L>(p)) * PS + i, f[p]);
+        for (int q = 0; q < Q; ++q) f[q] = St::ld(buf + q * W + PAD + tx - (ODD ? L::c(q, 0) : 0));
+        collide_any<L, S>(f, P);
+#pragma unroll
+        for (int p = 0; p < Q; ++p) {
+            if (ODD) {
+                const int off = L::c(p, 0) + L::c(p, 1) * sy + L::c(p, 2) * sz;
+                St::st(pop + static_cast<size_t>(p) * PS + (i + off), f[p]);
+            } else {
+                St::st(pop + static_cast<size_t>(inv<L>(p)) * PS + i, f[p]);
+            }
         }
     }
 }
@@ -539,19 +588,19 @@ __device__ __forceinline__ void row_block(const StepParams<S>& P, int seg, int n
 // positions), so that the latency-bound edge work is spread over the whole launch instead of
 // holding the SMs at its start; the row blocks fill the other indices in order.
 template <class L, class S, bool ODD>
-__global__ void __launch_bounds__(kRowCells)
-    step_kernel(const StepParams<S> P, int n_edge_blocks, int edge_stride, int nseg_x)
+__global__ void __launch_bounds__(kRowCells, LBMG_MIN_BLOCKS)
+    step_kernel(const StepParams<S> P, int n_edge_blocks, int edge_stride, int nseg, int nseg_x)
 {
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    __shared__ __align__(8) uint64_t bar;
+    __shared__ __align__(8) uint64_t bars[kSegs];
     const int b = static_cast<int>(blockIdx.x);
     const int interleaved = n_edge_blocks * edge_stride;
     if (b < interleaved && b % edge_stride == 0)
         edge_block<L, S, ODD>(P, b / edge_stride, smem_raw);
     else if (b < interleaved)
-        row_block<L, S, ODD>(P, b - (b / edge_stride + 1), nseg_x, smem_raw, &bar);
+        row_block<L, S, ODD>(P, b - (b / edge_stride + 1), nseg, nseg_x, smem_raw, bars);
     else
-        row_block<L, S, ODD>(P, b - n_edge_blocks, nseg_x, smem_raw, &bar);
+        row_block<L, S, ODD>(P, b - n_edge_blocks, nseg, nseg_x, smem_raw, bars);
 }
 
 // ------------------------------------------------------------------------------------------

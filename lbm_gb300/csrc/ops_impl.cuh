@@ -20,7 +20,7 @@ inline unsigned linear_blocks(size_t n, unsigned threads)
     return static_cast<unsigned>(b < 65535u * 16u ? (b > 0 ? b : 1) : 65535u * 16u);
 }
 
-template <class S>
+template <class L, class S>
 StepParams<S> step_params(const DomainDev& d)
 {
     StepParams<S> p;
@@ -66,19 +66,29 @@ struct Launch {
 
     static void step(const DomainDev& d, long long t, cudaStream_t s)
     {
-        const StepParams<S> p = step_params<S>(d);
+        const StepParams<S> p = step_params<L, S>(d);
         const int nseg_x = (d.g.xl + kRowCells - 1) / kRowCells;
-        const long long nseg = static_cast<long long>(nseg_x) * d.g.yl * d.g.zl;
+        const int nseg = nseg_x * d.g.yl * d.g.zl;
+        const int row_blocks = (nseg + kSegs - 1) / kSegs;
         const int n_edge_blocks = (d.n_edge + kRowCells - 1) / kRowCells;
-        const long long total = n_edge_blocks + nseg;
+        const long long total = static_cast<long long>(n_edge_blocks) + row_blocks;
         const int edge_stride = n_edge_blocks > 0 ? static_cast<int>(total / n_edge_blocks) : 1;
         const unsigned blocks = static_cast<unsigned>(total);
         constexpr size_t smem = row_smem_bytes<L, S>();
-        static_assert(smem <= 48 * 1024, "step kernel shared memory above the default limit");
+        if constexpr (smem > 48 * 1024) {
+            static bool opted_in = false;
+            if (!opted_in) {
+                cudaFuncSetAttribute(step_kernel<L, S, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     static_cast<int>(smem));
+                cudaFuncSetAttribute(step_kernel<L, S, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     static_cast<int>(smem));
+                opted_in = true;
+            }
+        }
         if (t & 1)
-            step_kernel<L, S, true><<<blocks, kRowCells, smem, s>>>(p, n_edge_blocks, edge_stride, nseg_x);
+            step_kernel<L, S, true><<<blocks, kRowCells, smem, s>>>(p, n_edge_blocks, edge_stride, nseg, nseg_x);
         else
-            step_kernel<L, S, false><<<blocks, kRowCells, smem, s>>>(p, n_edge_blocks, edge_stride, nseg_x);
+            step_kernel<L, S, false><<<blocks, kRowCells, smem, s>>>(p, n_edge_blocks, edge_stride, nseg, nseg_x);
         side_passes(d, t, s);
     }
 
