@@ -109,6 +109,14 @@ int lbm_get_populations(lbm_domain* d, double* f);
  * handle's stream. Asynchronous: returns after the launches. */
 int lbm_step(lbm_domain* d, int64_t nsteps);
 
+/* Extension: lbm_step with a conservation monitor. Each step also reduces, inside the step kernel,
+ * the FP64 totals of the populations it pulled (the mass and momentum it started from: sum rho,
+ * sum j_x, sum j_y, sum j_z over interior fluid cells) and copies them asynchronously to
+ * totals[4*k .. 4*k+3] for the k-th step of the call. totals must hold 4*nsteps doubles and stay
+ * valid until the next synchronising call; page-locked host memory keeps the copies
+ * asynchronous. The totals are summed with atomics, so their last bits may differ between runs. */
+int lbm_step_monitored(lbm_domain* d, int64_t nsteps, double* totals);
+
 /* Density and velocity of every interior cell (Cell::density / Cell::velocity on
  * collide_field, vtk.hpp:62-73), computed on the device in FP64. rho: one double per interior
  * cell; u: three (may be NULL). Synchronises. */

@@ -25,6 +25,9 @@ using namespace lbmg;
 
 namespace {
 
+// Slots of the device ring that holds per-step monitor results until their copy to the host.
+constexpr int kMonRing = 1024;
+
 thread_local std::string g_create_error;
 
 struct CudaError : std::runtime_error {
@@ -128,14 +131,16 @@ struct lbm_domain {
     DevBuf<double> red;  // 4 * kReduceBlocks partials + 4 totals
     DevBuf<uint32_t> link;  // per-cell link words
     DevBuf<int> edge;       // kFluidEdge cells
-    DevBuf<int> errword;    // device error word + a counter
+    DevBuf<int> errword;    // device error word, a list counter
+    DevBuf<double> mon;     // step monitor accumulators
+    DevBuf<double> mon_ring;  // per-step monitor results, kMonRing slots of 4 doubles
 
     std::string err;
 
     ~lbm_domain()
     {
         pop.release(); flag.release(); bc.release(); profile.release();
-        gf_xyz.release(); gf_pop.release(); fs_link.release(); red.release(); link.release(); edge.release(); errword.release();
+        gf_xyz.release(); gf_pop.release(); fs_link.release(); red.release(); link.release(); edge.release(); errword.release(); mon.release(); mon_ring.release();
         if (stream) cudaStreamDestroy(stream);
     }
 
@@ -474,6 +479,10 @@ int lbm_create(lbm_domain** out, int q, int64_t xl, int64_t yl, int64_t zl, doub
         d->errword.alloc(2, "cudaMalloc(error word)");
         check(cudaMemsetAsync(d->errword.p, 0, 2 * sizeof(int), d->stream), "clear error word");
         d->dev.err = d->errword.p;
+        d->mon.alloc(4 * kMonBuckets, "cudaMalloc(step monitor)");
+        check(cudaMemsetAsync(d->mon.p, 0, d->mon.bytes(), d->stream), "clear step monitor");
+        d->dev.mon = d->mon.p;
+        d->mon_ring.alloc(4 * kMonRing, "cudaMalloc(step monitor ring)");
         d->dev.pop = d->pop.p;
         d->dev.flag = d->flag.p;
         d->dev.bc = d->bc.p;
@@ -631,7 +640,25 @@ int lbm_step(lbm_domain* d, int64_t nsteps)
     return guarded(d, [&] {
         if (nsteps < 0) throw ArgError("nsteps must be >= 0");
         d->finalize();
-        for (int64_t k = 0; k < nsteps; ++k) d->ops->step(d->dev, d->steps + 1 + k, d->stream);
+        for (int64_t k = 0; k < nsteps; ++k) d->ops->step(d->dev, d->steps + 1 + k, nullptr, d->stream);
+        check(cudaGetLastError(), "step kernel launch");
+        d->steps += nsteps;
+        if (nsteps > 0) d->state_custom = true;
+    });
+}
+
+int lbm_step_monitored(lbm_domain* d, int64_t nsteps, double* totals)
+{
+    return guarded(d, [&] {
+        if (nsteps < 0) throw ArgError("nsteps must be >= 0");
+        if (!totals && nsteps > 0) throw ArgError("totals is NULL");
+        d->finalize();
+        for (int64_t k = 0; k < nsteps; ++k) {
+            double* slot = d->mon_ring.p + 4 * (k % kMonRing);
+            d->ops->step(d->dev, d->steps + 1 + k, slot, d->stream);
+            check(cudaMemcpyAsync(totals + 4 * k, slot, 4 * sizeof(double), cudaMemcpyDeviceToHost, d->stream),
+                  "copy step totals");
+        }
         check(cudaGetLastError(), "step kernel launch");
         d->steps += nsteps;
         if (nsteps > 0) d->state_custom = true;
@@ -705,7 +732,7 @@ int lbm_memory_info(const lbm_domain* d, uint64_t* device_bytes, uint64_t* step_
         m->finalize();
         if (device_bytes)
             *device_bytes = m->pop.bytes() + m->flag.bytes() + m->bc.bytes() + m->profile.bytes() + m->gf_xyz.bytes() +
-                            m->gf_pop.bytes() + m->fs_link.bytes() + m->red.bytes() + m->link.bytes() + m->edge.bytes() + m->errword.bytes();
+                            m->gf_pop.bytes() + m->fs_link.bytes() + m->red.bytes() + m->link.bytes() + m->edge.bytes() + m->errword.bytes() + m->mon.bytes() + m->mon_ring.bytes();
         if (step_bytes) *step_bytes = 2ull * m->Q * store_bytes(m->precision) * m->fluid_cells;
         if (fluid_cells) *fluid_cells = m->fluid_cells;
         if (launches_per_step)

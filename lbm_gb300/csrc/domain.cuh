@@ -40,6 +40,8 @@ enum CellFlag : uint8_t {
     kFirstHandler = 3 // kFirstHandler + h - 1 : non-fluid cell bound to handler h (1-based)
 };
 constexpr int kMaxHandlers = 250;
+// Accumulator buckets of the step monitor (atomics of different warps spread over them).
+constexpr int kMonBuckets = 256;
 
 // Boundary-handler types (values match LBM_NOSLIP ... LBM_PRESSURE in lbm_gb300.h).
 enum BcType : int {
@@ -88,6 +90,8 @@ struct DomainDev {
     int n_edge;
     // Device error word: set to 1 by a kernel whose bounded wait gave up.
     int* err;
+    // Step monitor accumulators (kMonBuckets x 4 doubles, zero between steps).
+    double* mon;
 };
 
 // A free-slip link: after a step, plane `q` at fluid cell `dst` receives the post-collision

@@ -162,12 +162,16 @@ __device__ __forceinline__ double feq_exact(int q, double rho, double u0, double
 
 // BGKCollision::collide (collision.hpp:60-70).
 template <class L>
-__device__ __forceinline__ void collide_exact(double (&f)[L::Q], double tau)
+__device__ __forceinline__ void collide_exact(double (&f)[L::Q], double tau, double (&m)[4])
 {
     const double rho = density_exact<L>(f);
-    const double u0 = momentum_exact<L>(f, 0) / rho;
-    const double u1 = momentum_exact<L>(f, 1) / rho;
-    const double u2 = momentum_exact<L>(f, 2) / rho;
+    m[0] = rho;
+    m[1] = momentum_exact<L>(f, 0);
+    m[2] = momentum_exact<L>(f, 1);
+    m[3] = momentum_exact<L>(f, 2);
+    const double u0 = m[1] / rho;
+    const double u1 = m[2] / rho;
+    const double u2 = m[3] / rho;
 #pragma unroll
     for (int q = 0; q < L::Q; ++q) {
         const double feq = feq_exact<L>(q, rho, u0, u1, u2);
@@ -258,10 +262,14 @@ __device__ __forceinline__ void moments_shifted(const float (&s)[L::Q], float& d
 // sym = drho - rho uu/(2 cs2) + rho cu^2/(2 cs4) and differ in the sign of asym = rho cu/cs2:
 //   s_eq,q - ... = w_q (sym +- asym),   s_q <- s_q + omega (w_q (sym +- asym) - s_q).
 template <class L>
-__device__ __forceinline__ void collide_shifted(float (&s)[L::Q], float omega)
+__device__ __forceinline__ void collide_shifted(float (&s)[L::Q], float omega, double (&m)[4])
 {
     float drho, jx, jy, jz;
     moments_shifted<L>(s, drho, jx, jy, jz);
+    m[0] = 1.0 + static_cast<double>(drho);
+    m[1] = jx;
+    m[2] = jy;
+    m[3] = jz;
     const float rho = 1.f + drho;
     const float ir = __frcp_rn(rho);
     const float ux = jx * ir, uy = jy * ir, uz = jz * ir;
@@ -333,18 +341,36 @@ struct StepParams {
     const int* edge;       // layout indices of the kFluidEdge cells, increasing
     int n_edge;
     int* err;              // set to 1 when a bounded wait gives up
+    double* mon;           // kMonBuckets x 4 FP64 accumulators of the step's mass and momentum,
+                           // or nullptr
     Geom g;
     double tau;
     float omega;
 };
 
+// Collides f in place; m receives the mass and momentum of the populations it started from.
 template <class L, class S>
-__device__ __forceinline__ void collide_any(typename Store<S>::C (&f)[L::Q], const StepParams<S>& P)
+__device__ __forceinline__ void collide_any(typename Store<S>::C (&f)[L::Q], const StepParams<S>& P, double (&m)[4])
 {
     if constexpr (Store<S>::kShifted)
-        collide_shifted<L>(f, P.omega);
+        collide_shifted<L>(f, P.omega, m);
     else
-        collide_exact<L>(f, P.tau);
+        collide_exact<L>(f, P.tau, m);
+}
+
+// Adds the warp's totals of m to one accumulator bucket. Every lane of the warp must call it.
+__device__ __forceinline__ void monitor_add(double* mon, const double (&m)[4])
+{
+    double v[4] = {m[0], m[1], m[2], m[3]};
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+        for (int k = 0; k < 4; ++k) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+    if ((threadIdx.x & 31) == 0) {
+        double* b = mon + 4 * ((blockIdx.x * 4 + (threadIdx.x >> 5)) % kMonBuckets);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) atomicAdd(b + k, v[k]);
+    }
 }
 
 // Handler values of an edge cell: for every direction p toward a non-fluid neighbour (bit inv(p)
@@ -437,9 +463,14 @@ __device__ __forceinline__ void store_edge_populations(const StepParams<S>& P, i
 #ifndef LBMG_SEGS
 #define LBMG_SEGS 1
 #endif
-#ifndef LBMG_MIN_BLOCKS
-#define LBMG_MIN_BLOCKS 1
-#endif
+// Resident blocks per SM the compiler must allow (register cap 65536 / (128 * n)): 12 for the
+// FP32-arithmetic D3Q15 / D3Q19 kernels, whose row blocks then keep more copies in flight; none
+// for D3Q27 and FP64, which would spill under that cap.
+template <class L, class S>
+constexpr int step_min_blocks()
+{
+    return (sizeof(S) <= 4 && sizeof(typename Store<S>::C) == 4 && L::Q <= 19) ? 12 : 1;
+}
 constexpr int kRowCells = LBMG_ROW_CELLS;
 constexpr int kSegs = LBMG_SEGS;
 constexpr uint32_t kMaxPolls = 1u << 20;
@@ -472,33 +503,36 @@ __device__ __forceinline__ void edge_block(const StepParams<S>& P, int blk, unsi
     constexpr int Q = L::Q;
     const int tx = static_cast<int>(threadIdx.x);
     const int j = blk * kRowCells + tx;
-    if (j >= P.n_edge) return;
-    const int i = P.edge[j];
-    const int r = i - kXOff;
-    const int x = r % P.g.XS;
-    const int t = r / P.g.XS;
-    const int y = t % P.g.YS, z = t / P.g.YS;
-    const uint32_t link = P.link[i];
-    S* __restrict__ pop = P.pop;
-    T f[Q];
+    double m[4] = {0.0, 0.0, 0.0, 0.0};
+    if (j < P.n_edge) {
+        const int i = P.edge[j];
+        const int r = i - kXOff;
+        const int x = r % P.g.XS;
+        const int t = r / P.g.XS;
+        const int y = t % P.g.YS, z = t / P.g.YS;
+        const uint32_t link = P.link[i];
+        S* __restrict__ pop = P.pop;
+        T f[Q];
 #pragma unroll
-    for (int q = 0; q < Q; ++q) {
-        if (!ODD || ((link >> q) & 1u)) {
-            f[q] = St::ld(pop + static_cast<size_t>(q) * P.g.PS + i);
-        } else {
-            int nx, ny, nz;
-            nbr_xyz(P.g, x, y, z, -L::c(q, 0), -L::c(q, 1), -L::c(q, 2), nx, ny, nz);
-            f[q] = St::ld(pop + static_cast<size_t>(inv<L>(q)) * P.g.PS + cidx(P.g, nx, ny, nz));
+        for (int q = 0; q < Q; ++q) {
+            if (!ODD || ((link >> q) & 1u)) {
+                f[q] = St::ld(pop + static_cast<size_t>(q) * P.g.PS + i);
+            } else {
+                int nx, ny, nz;
+                nbr_xyz(P.g, x, y, z, -L::c(q, 0), -L::c(q, 1), -L::c(q, 2), nx, ny, nz);
+                f[q] = St::ld(pop + static_cast<size_t>(inv<L>(q)) * P.g.PS + cidx(P.g, nx, ny, nz));
+            }
+        }
+        collide_any<L, S>(f, P, m);
+        store_edge_populations<L, S, ODD>(P, x, y, z, i, link, f);
+        if (link & ((1u << Q) - 1u)) {
+            T* fs = reinterpret_cast<T*>(smem_raw) + tx;
+#pragma unroll
+            for (int q = 0; q < Q; ++q) fs[q * kRowCells] = f[q];
+            store_handler_values<L, S>(P, x, y, z, i, link, fs, kRowCells);
         }
     }
-    collide_any<L, S>(f, P);
-    store_edge_populations<L, S, ODD>(P, x, y, z, i, link, f);
-    if (link & ((1u << Q) - 1u)) {
-        T* fs = reinterpret_cast<T*>(smem_raw) + tx;
-#pragma unroll
-        for (int q = 0; q < Q; ++q) fs[q * kRowCells] = f[q];
-        store_handler_values<L, S>(P, x, y, z, i, link, fs, kRowCells);
-    }
+    if (P.mon) monitor_add(P.mon, m);
 }
 
 __device__ __forceinline__ void segment_origin(const Geom& g, int seg, int nseg_x, int& x0, int& y, int& z)
@@ -559,28 +593,31 @@ __device__ __forceinline__ void row_block(const StepParams<S>& P, int rb, int ns
         segment_origin(P.g, seg0 + s, nseg_x, x0, y, z);
         const int x = x0 + tx;
         const int i = cidx(P.g, x, y, z);
-        const bool bulk = x <= P.g.xl && P.flag[i] == kFluidBulk;
+        bool bulk = x <= P.g.xl && P.flag[i] == kFluidBulk;
         if (!mbar_wait_bounded(&bars[s], 0, kMaxPolls)) {
+            // the step's results are invalid; still never leave while copies may land here
             *P.err = 1;
-            // never leave while copies may still land in this block's shared memory
-            for (int r = s; r < nsegs; ++r) mbar_wait_bounded(&bars[r], 0, kMaxPolls);
-            return;
+            mbar_wait_bounded(&bars[s], 0, kMaxPolls);
+            bulk = false;
         }
-        if (!bulk) continue;
-        const S* buf = reinterpret_cast<const S*>(smem_raw + s * SB);
-        T f[Q];
+        double m[4] = {0.0, 0.0, 0.0, 0.0};
+        if (bulk) {
+            const S* buf = reinterpret_cast<const S*>(smem_raw + s * SB);
+            T f[Q];
 #pragma unroll
-        for (int q = 0; q < Q; ++q) f[q] = St::ld(buf + q * W + PAD + tx - (ODD ? L::c(q, 0) : 0));
-        collide_any<L, S>(f, P);
+            for (int q = 0; q < Q; ++q) f[q] = St::ld(buf + q * W + PAD + tx - (ODD ? L::c(q, 0) : 0));
+            collide_any<L, S>(f, P, m);
 #pragma unroll
-        for (int p = 0; p < Q; ++p) {
-            if (ODD) {
-                const int off = L::c(p, 0) + L::c(p, 1) * sy + L::c(p, 2) * sz;
-                St::st(pop + static_cast<size_t>(p) * PS + (i + off), f[p]);
-            } else {
-                St::st(pop + static_cast<size_t>(inv<L>(p)) * PS + i, f[p]);
+            for (int p = 0; p < Q; ++p) {
+                if (ODD) {
+                    const int off = L::c(p, 0) + L::c(p, 1) * sy + L::c(p, 2) * sz;
+                    St::st(pop + static_cast<size_t>(p) * PS + (i + off), f[p]);
+                } else {
+                    St::st(pop + static_cast<size_t>(inv<L>(p)) * PS + i, f[p]);
+                }
             }
         }
+        if (P.mon) monitor_add(P.mon, m);
     }
 }
 
@@ -588,7 +625,7 @@ __device__ __forceinline__ void row_block(const StepParams<S>& P, int rb, int ns
 // positions), so that the latency-bound edge work is spread over the whole launch instead of
 // holding the SMs at its start; the row blocks fill the other indices in order.
 template <class L, class S, bool ODD>
-__global__ void __launch_bounds__(kRowCells, LBMG_MIN_BLOCKS)
+__global__ void __launch_bounds__(kRowCells, (step_min_blocks<L, S>()))
     step_kernel(const StepParams<S> P, int n_edge_blocks, int edge_stride, int nseg, int nseg_x)
 {
     extern __shared__ __align__(128) unsigned char smem_raw[];

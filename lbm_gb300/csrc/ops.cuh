@@ -14,8 +14,9 @@ struct KernelOps {
     void (*init)(const DomainDev& d, cudaStream_t s);
     // fluid cells -> kFluidBulk / kFluidEdge
     void (*classify)(const DomainDev& d, cudaStream_t s);
-    // one time step number `t` (1-based): fused kernel, then the side passes
-    void (*step)(const DomainDev& d, long long t, cudaStream_t s);
+    // one time step number `t` (1-based): fused kernel, then the side passes; with mon_out
+    // (device, 4 doubles) also the FP64 mass and momentum the step started from
+    void (*step)(const DomainDev& d, long long t, double* mon_out, cudaStream_t s);
     // state after `k` steps -> AoS FP64 over all cells (device buffer)
     void (*gather)(const DomainDev& d, long long k, double* out, cudaStream_t s);
     // AoS FP64 over all cells (device buffer) -> state after `k` steps

@@ -33,6 +33,7 @@ StepParams<S> step_params(const DomainDev& d)
     p.profile = d.profile;
     p.g = d.g;
     p.err = d.err;
+    p.mon = nullptr;
     p.tau = d.tau;
     p.omega = static_cast<float>(1.0 / d.tau);
     return p;
@@ -64,9 +65,10 @@ struct Launch {
                 pop, d.flag, d.g, d.fs_link, d.n_fs, copy, d.gf_pop, d.n_gf, copy);
     }
 
-    static void step(const DomainDev& d, long long t, cudaStream_t s)
+    static void step(const DomainDev& d, long long t, double* mon_out, cudaStream_t s)
     {
-        const StepParams<S> p = step_params<L, S>(d);
+        StepParams<S> p = step_params<L, S>(d);
+        p.mon = mon_out ? d.mon : nullptr;
         const int nseg_x = (d.g.xl + kRowCells - 1) / kRowCells;
         const int nseg = nseg_x * d.g.yl * d.g.zl;
         const int row_blocks = (nseg + kSegs - 1) / kSegs;
@@ -89,6 +91,7 @@ struct Launch {
             step_kernel<L, S, true><<<blocks, kRowCells, smem, s>>>(p, n_edge_blocks, edge_stride, nseg, nseg_x);
         else
             step_kernel<L, S, false><<<blocks, kRowCells, smem, s>>>(p, n_edge_blocks, edge_stride, nseg, nseg_x);
+        if (mon_out) monitor_final_kernel<<<1, 256, 0, s>>>(d.mon, mon_out);
         side_passes(d, t, s);
     }
 

@@ -165,6 +165,20 @@ __global__ void __launch_bounds__(kReduceThreads)
     }
 }
 
+// Sums the step monitor's accumulator buckets in a fixed order into out[4] and clears them for the
+// next step.
+static __global__ void monitor_final_kernel(double* buckets, double* out)
+{
+    const int k = static_cast<int>(threadIdx.x);
+    if (k < 4) {
+        double v = 0.0;
+        for (int b = 0; b < kMonBuckets; ++b) v += buckets[4 * b + k];
+        out[k] = v;
+    }
+    __syncthreads();
+    for (int j = k; j < 4 * kMonBuckets; j += blockDim.x) buckets[j] = 0.0;
+}
+
 static __global__ void reduce_final_kernel(const double* partials, int nblocks, double* out)
 {
     if (threadIdx.x < 4) {
@@ -191,7 +205,8 @@ __global__ void ghost_fluid_kernel(S* pop, const uint8_t* flag, Geom g, double t
     double f[L::Q];
 #pragma unroll
     for (int q = 0; q < L::Q; ++q) f[q] = c[q];
-    collide_exact<L>(f, tau);
+    double m[4];
+    collide_exact<L>(f, tau, m);
     const int x = gf_xyz[3 * j], y = gf_xyz[3 * j + 1], z = gf_xyz[3 * j + 2];
 #pragma unroll
     for (int q = 0; q < L::Q; ++q) {

@@ -239,6 +239,14 @@ class Domain:
         """nsteps x {stream(); swap(); collide();} in one call (asynchronous)."""
         check(self._lib.lbm_step(self._h, int(nsteps)), self._h)
 
+    def step_monitored(self, nsteps: int, totals: np.ndarray | None = None) -> np.ndarray:
+        """Extension: nsteps steps, each reporting the FP64 mass and momentum it started from
+        (array (nsteps, 4)); valid after sync()."""
+        out = totals if totals is not None else np.empty((int(nsteps), 4), dtype=np.float64)
+        check(self._lib.lbm_step_monitored(self._h, int(nsteps), out.ctypes.data), self._h)
+        self._monitor_keepalive = out
+        return out
+
     def sync(self) -> None:
         check(self._lib.lbm_sync(self._h), self._h)
 

@@ -215,3 +215,33 @@ def test_reduced_precision_channel(precision, q):
     print(f"{precision} q{q}: u rel L2 {eu:.3e}, rho rel L2 {er:.3e}")
     assert eu <= TOL_U[precision]
     assert er <= TOL_RHO[precision]
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_step_monitor_matches_reduction(precision):
+    # closed no-slip box: every population a fluid cell pulls is some fluid cell's post-collision
+    # value, so the totals a step starts from equal the totals after the previous step
+    scn = S.cavity(14, q=19, lid=0.0, ny=11, nz=9)
+    rng = np.random.default_rng(3)
+    scn.init = np.tile(scn.model.weights, (scn.ncells, 1)) * (1 + 0.02 * rng.standard_normal((scn.ncells, 19)))
+    with build_domain(scn, precision) as dom:
+        dom.step(5)
+        before = dom.reduce_mass_momentum()
+        tot = dom.step_monitored(3)
+        dom.sync()
+        after = dom.reduce_mass_momentum()
+    tol = 1e-12 if precision == "fp64" else 1e-6
+    assert abs(tot[0, 0] - before[0]) <= tol * before[0]
+    assert np.allclose(tot[0, 1:], before[1:], atol=tol * before[0])
+    assert abs(tot[2, 0] - tot[0, 0]) <= 10 * tol * before[0]
+    assert abs(after[0] - tot[0, 0]) <= 10 * tol * before[0]
+
+
+def test_step_monitor_counts_like_plain_steps():
+    scn = S.channel(20, 10, 10, q=19, sphere=((8, 5, 5), 2))
+    with build_domain(scn, "fp32") as a, build_domain(scn, "fp32") as b:
+        a.step(12)
+        b.step_monitored(12)
+        b.sync()
+        assert a.steps_done == b.steps_done == 12
+        assert np.array_equal(a.populations(), b.populations())
