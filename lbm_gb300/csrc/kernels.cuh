@@ -463,14 +463,6 @@ __device__ __forceinline__ void store_edge_populations(const StepParams<S>& P, i
 #ifndef LBMG_SEGS
 #define LBMG_SEGS 1
 #endif
-// Resident blocks per SM the compiler must allow (register cap 65536 / (128 * n)): 12 for the
-// FP32-arithmetic D3Q15 / D3Q19 kernels, whose row blocks then keep more copies in flight; none
-// for D3Q27 and FP64, which would spill under that cap.
-template <class L, class S>
-constexpr int step_min_blocks()
-{
-    return (sizeof(S) <= 4 && sizeof(typename Store<S>::C) == 4 && L::Q <= 19) ? 12 : 1;
-}
 constexpr int kRowCells = LBMG_ROW_CELLS;
 constexpr int kSegs = LBMG_SEGS;
 constexpr uint32_t kMaxPolls = 1u << 20;
@@ -625,7 +617,7 @@ __device__ __forceinline__ void row_block(const StepParams<S>& P, int rb, int ns
 // positions), so that the latency-bound edge work is spread over the whole launch instead of
 // holding the SMs at its start; the row blocks fill the other indices in order.
 template <class L, class S, bool ODD>
-__global__ void __launch_bounds__(kRowCells, (step_min_blocks<L, S>()))
+__global__ void __launch_bounds__(kRowCells)
     step_kernel(const StepParams<S> P, int n_edge_blocks, int edge_stride, int nseg, int nseg_x)
 {
     extern __shared__ __align__(128) unsigned char smem_raw[];

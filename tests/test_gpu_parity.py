@@ -194,8 +194,8 @@ def test_bad_arguments_on_device():
 # Reduced precision: FP32 arithmetic on shifted FP32 / FP16 / BF16 storage against FP64.
 # Tolerances (relative L2 over interior fluid cells) are stated here and in the design doc.
 # ------------------------------------------------------------------------------------------
-TOL_U = {"fp32": 1e-5, "fp16": 2e-2, "bf16": 1e-1}
-TOL_RHO = {"fp32": 1e-7, "fp16": 1e-4, "bf16": 1e-3}
+TOL_U = {"fp32": 5e-6, "fp16": 2e-3, "bf16": 2e-2}
+TOL_RHO = {"fp32": 2e-7, "fp16": 5e-5, "bf16": 5e-4}
 
 
 @pytest.mark.parametrize("precision", ["fp32", "fp16", "bf16"])
@@ -218,12 +218,18 @@ def test_reduced_precision_channel(precision, q):
 
 
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])
-def test_step_monitor_matches_reduction(precision):
-    # closed no-slip box: every population a fluid cell pulls is some fluid cell's post-collision
-    # value, so the totals a step starts from equal the totals after the previous step
-    scn = S.cavity(14, q=19, lid=0.0, ny=11, nz=9)
-    rng = np.random.default_rng(3)
-    scn.init = np.tile(scn.model.weights, (scn.ncells, 1)) * (1 + 0.02 * rng.standard_normal((scn.ncells, 19)))
+@pytest.mark.parametrize("periodic", [False, True])
+def test_step_monitor_matches_reduction(precision, periodic):
+    # Every population a fluid cell pulls is some fluid cell's post-collision value (bounce-back
+    # returns it to its own cell), so the mass a step starts from is the mass after the previous
+    # step. Momentum too on a periodic box; walls reverse the momentum of bounced populations.
+    if periodic:
+        scn = S.taylor_green(12, u0=0.04, omega=1.6, q=19)
+        scn.init = scn.init * (1 + 0.01 * np.random.default_rng(4).standard_normal(scn.init.shape))
+    else:
+        scn = S.cavity(14, q=19, lid=0.0, ny=11, nz=9)
+        rng = np.random.default_rng(3)
+        scn.init = np.tile(scn.model.weights, (scn.ncells, 1)) * (1 + 0.02 * rng.standard_normal((scn.ncells, 19)))
     with build_domain(scn, precision) as dom:
         dom.step(5)
         before = dom.reduce_mass_momentum()
@@ -232,9 +238,10 @@ def test_step_monitor_matches_reduction(precision):
         after = dom.reduce_mass_momentum()
     tol = 1e-12 if precision == "fp64" else 1e-6
     assert abs(tot[0, 0] - before[0]) <= tol * before[0]
-    assert np.allclose(tot[0, 1:], before[1:], atol=tol * before[0])
     assert abs(tot[2, 0] - tot[0, 0]) <= 10 * tol * before[0]
     assert abs(after[0] - tot[0, 0]) <= 10 * tol * before[0]
+    if periodic:
+        assert np.allclose(tot[0, 1:], before[1:], rtol=0, atol=10 * tol * before[0])
 
 
 def test_step_monitor_counts_like_plain_steps():
