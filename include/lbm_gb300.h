@@ -122,6 +122,24 @@ int lbm_step_monitored(lbm_domain* d, int64_t nsteps, double* totals);
  * cell; u: three (may be NULL). Synchronises. */
 int lbm_moments(lbm_domain* d, double* rho, double* u);
 
+/* No counterpart in the reference: lbm_moments for callers that must not allocate device memory.
+ * Same results as lbm_moments (the same kernel), but the device buffer that holds the moments on
+ * their way to the host is a static array inside the library (8 MiB, at most 262144 interior
+ * cells; larger domains are rejected with LBM_ERR_ARG) instead of a cudaMalloc / cudaFree pair
+ * per call. For callers whose device memory is owned by their own pool allocator (a cudaMalloc
+ * would fail once the pool holds all free memory, or would make the pool give memory back), and
+ * for loops that read the moments every step (the reference driver's timesteps-per-plot = 1),
+ * where each cudaMalloc / cudaFree would synchronise the whole device.
+ *   - The first call on a device looks up the array's device address (cudaGetSymbolAddress);
+ *     make that first call before any stream capture.
+ *   - All calls in the process share the array: calls whose work overlaps on the GPU (two handles
+ *     on different streams) race. Each call writes every element it reads back, so nothing
+ *     carries over from the previous call.
+ *   - Returns LBM_ERR_STATE when the geometry changed since the last step (applying the change
+ *     may allocate); any call that steps or reads the state applies it first.
+ * The array stays allocated in every GPU that loads the library until the process exits. */
+int lbm_moments_noalloc(lbm_domain* d, double* rho, double* u);
+
 /* Extension: FP64 totals over interior fluid cells of the post-collision populations:
  * out = {sum rho, sum j_x, sum j_y, sum j_z}. Returns LBM_ERR_DIVERGED (after filling out) when
  * any total is not finite. Synchronises. */

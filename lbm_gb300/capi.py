@@ -56,6 +56,7 @@ SIGNATURES = {
     "lbm_step": (ctypes.c_int, [_P, _I64]),
     "lbm_step_monitored": (ctypes.c_int, [_P, _I64, _P]),
     "lbm_moments": (ctypes.c_int, [_P, _P, _P]),
+    "lbm_moments_noalloc": (ctypes.c_int, [_P, _P, _P]),
     "lbm_reduce_mass_momentum": (ctypes.c_int, [_P, _P]),
     "lbm_sync": (ctypes.c_int, [_P]),
     "lbm_get_stream": (ctypes.c_int, [_P, ctypes.POINTER(_P)]),

@@ -11,6 +11,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <stdexcept>
 #include <string>
@@ -109,6 +110,7 @@ struct lbm_domain {
     cudaStream_t stream = nullptr;
     int Q = 0;
     int precision = 0;
+    int device = 0;         // device current at lbm_create
     size_t ng = 0;         // cells incl. ghost layer
     size_t n_interior = 0;
     uint64_t fluid_cells = 0;
@@ -396,6 +398,31 @@ void lbm_domain::finalize()
 
 namespace {
 
+// Device scratch of lbm_moments_noalloc: density and velocity of up to kNoAllocMaxCells interior
+// cells (4 doubles each, 8 MiB). It lives in every GPU that loads the library until the process
+// exits, and all calls share it.
+constexpr size_t kNoAllocMaxCells = 262144;
+static __device__ __align__(256) double g_noalloc_moments[4 * kNoAllocMaxCells];
+
+// Its device address, looked up once per device (with that device current) by the first
+// lbm_moments_noalloc call on that device. The host-side name of the array is not a device
+// address and is never handed to a kernel.
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+double* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+
+double* noalloc_scratch(int device)
+{
+    if (device < 0 || device >= kNoAllocMaxDevices) throw ArgError("device ordinal out of range");
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_ptr[device]) {
+        void* p = nullptr;
+        check(cudaGetSymbolAddress(&p, g_noalloc_moments), "cudaGetSymbolAddress(no-alloc scratch)");
+        g_noalloc_ptr[device] = static_cast<double*>(p);
+    }
+    return g_noalloc_ptr[device];
+}
+
 template <class F>
 int guarded(lbm_domain* d, F&& f)
 {
@@ -469,6 +496,7 @@ int lbm_create(lbm_domain** out, int q, int64_t xl, int64_t yl, int64_t zl, doub
         case LBM_FP16: d->ops = ops_fp16(q); break;
         default: d->ops = ops_bf16(q); break;
         }
+        check(cudaGetDevice(&d->device), "cudaGetDevice");
         check(cudaStreamCreateWithFlags(&d->stream, cudaStreamNonBlocking), "cudaStreamCreate");
         d->pop.alloc(static_cast<size_t>(q) * g.PS * store_bytes(precision), "cudaMalloc(populations)");
         d->flag.alloc(g.PS, "cudaMalloc(flags)");
@@ -678,6 +706,37 @@ int lbm_moments(lbm_domain* d, double* rho, double* u)
               "download density");
         if (u)
             check(cudaMemcpyAsync(u, tmp.p + d->n_interior, 3 * d->n_interior * sizeof(double),
+                                  cudaMemcpyDeviceToHost, d->stream),
+                  "download velocity");
+        check(cudaStreamSynchronize(d->stream), "moments");
+        d->check_device_error();
+    });
+}
+
+int lbm_moments_noalloc(lbm_domain* d, double* rho, double* u)
+{
+    return guarded(d, [&] {
+        if (!rho) throw ArgError("rho is NULL");
+        if (d->geom_dirty)
+            throw StateError("the geometry changed since the last step; call lbm_step (or lbm_moments) once before "
+                             "lbm_moments_noalloc, which never allocates and so cannot apply the change");
+        if (d->n_interior > kNoAllocMaxCells)
+            throw ArgError("lbm_moments_noalloc handles at most 262144 interior cells (its static device scratch); "
+                           "this domain has " + std::to_string(d->n_interior) + ": use lbm_moments");
+        int prev = -1;
+        check(cudaGetDevice(&prev), "cudaGetDevice");
+        if (prev != d->device) check(cudaSetDevice(d->device), "cudaSetDevice");
+        struct Restore {
+            int dev, prev;
+            ~Restore() { if (prev >= 0 && prev != dev) cudaSetDevice(prev); }
+        } restore{d->device, prev};
+        double* scratch = noalloc_scratch(d->device);
+        d->ops->moments(d->dev, d->steps, scratch, u ? scratch + d->n_interior : nullptr, d->stream);
+        check(cudaGetLastError(), "moments kernel");
+        check(cudaMemcpyAsync(rho, scratch, d->n_interior * sizeof(double), cudaMemcpyDeviceToHost, d->stream),
+              "download density");
+        if (u)
+            check(cudaMemcpyAsync(u, scratch + d->n_interior, 3 * d->n_interior * sizeof(double),
                                   cudaMemcpyDeviceToHost, d->stream),
                   "download velocity");
         check(cudaStreamSynchronize(d->stream), "moments");
