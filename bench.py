@@ -248,10 +248,81 @@ def run_ours(args, rank, world, local):
     }
     line.update(out_extra)
     if not args.quick:
+        line["adjoint"] = run_adjoint()
         line["e2e"] = run_e2e(scn19, K, W)
         if rank == 0:
             line["cpu_baseline"] = cpu_baseline(size, budget_s=12.0)
     return line if rank == 0 else None
+
+
+def run_adjoint(xl=128, yl=64, zl=64, steps=2000, ckpt=100):
+    """Gradient workload: D3Q19 channel 128x64x64, per-cell inlet profile u_x ~ U[0.02, 0.05] and 5 %
+    random solids from seed 0, omega 1.7, 2000 steps, checkpoints every 100 steps, objective = kinetic
+    energy in x in [96, 128) (interior cells 97..128). FP32 forward + adjoint; plain FP32 steps timed
+    beside it; the FP32 and FP64 adjoint gradients at three inlet cells against FP64 central finite
+    differences (h = 1e-5)."""
+    import torch
+    from lbm_gb300 import build_domain
+    from lbm_gb300 import scenario as S
+    scn = S.adjoint_channel(xl, yl, zl, omega=1.7, seed=0)
+    box = (97, xl, 1, yl, 1, zl)
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = fn()
+        torch.cuda.synchronize()
+        return time.perf_counter() - t0, r
+
+    with build_domain(scn, "fp32") as d:
+        plain = time_steps(d, steps, 5)
+    with build_domain(scn, "fp32") as d:
+        d.step(0)
+        d.sync()
+        fwd, _ = timed(lambda: (d.adjoint_forward(steps, ckpt), d.sync()))
+        J32 = d.objective_ke(box)
+        bwd, (g32, _) = timed(lambda: d.adjoint_backward(box))
+        bwd2, _ = timed(lambda: d.adjoint_backward(box))  # allocations warm
+    bwd = min(bwd, bwd2)
+    with build_domain(scn, "fp64") as d:
+        d.adjoint_forward(steps, ckpt)
+        J64 = d.objective_ke(box)
+        g64, _ = d.adjoint_backward(box)
+    h = 1e-5
+    cells = [(32, 32), (10, 50), (60, 5)]
+    errs32, errs64, fds = [], [], []
+    for (y, z) in cells:
+        k = (z * (yl + 2) + y) * (xl + 2)
+        vals = []
+        for sgn in (1, -1):
+            s2 = S.adjoint_channel(xl, yl, zl, omega=1.7, seed=0)
+            s2.boundaries[0].profile = s2.boundaries[0].profile.copy()
+            s2.boundaries[0].profile[k, 0] += sgn * h
+            with build_domain(s2, "fp64") as d:
+                d.step(steps)
+                vals.append(d.objective_ke(box))
+        fd = (vals[0] - vals[1]) / (2 * h)
+        fds.append(fd)
+        errs32.append(abs(g32[k, 0] - fd) / abs(fd))
+        errs64.append(abs(g64[k, 0] - fd) / abs(fd))
+    n = scn.ninterior
+    return {
+        "workload": f"adjoint channel D3Q19 {xl}x{yl}x{zl}, inlet profile + 5% solids from seed 0, omega 1.7, "
+                    f"{steps} steps, checkpoint every {ckpt}, J = KE in x in [96,{xl})",
+        "storage": "fp32 (f - w)", "steps": steps, "ckpt_every": ckpt,
+        "forward_plain_ms_per_step": plain / steps * 1e3,
+        "forward_ckpt_ms_per_step": fwd / steps * 1e3,
+        "backward_ms_per_step": bwd / steps * 1e3,
+        "backward_over_forward": bwd / plain,
+        "forward_plus_backward_over_forward": (fwd + bwd) / plain,
+        "forward_mlups": n * steps / plain / 1e6,
+        "J_fp32": J32, "J_fp64": J64,
+        "fd_check": {"param": "inlet u_x at (y, z)", "cells": cells, "fd_fp64": fds,
+                     "max_rel_err_fp32_adjoint": max(errs32), "max_rel_err_fp64_adjoint": max(errs64),
+                     "h": h},
+        "timing": "wall clock around synchronised calls (backward includes its allocations and the "
+                  "gradient download); plain steps by CUDA events",
+    }
 
 
 def run_e2e(scn, K, W):

@@ -145,6 +145,30 @@ int lbm_moments_noalloc(lbm_domain* d, double* rho, double* u);
  * any total is not finite. Synchronises. */
 int lbm_reduce_mass_momentum(lbm_domain* d, double out[4]);
 
+/* Extension (no reference counterpart): gradients by a hand-written discrete adjoint of the step.
+ * Forward: nsteps steps from the current state, keeping a copy of the state every ckpt_every
+ * steps (device memory: ceil(nsteps / ckpt_every) copies of the population store). Not available
+ * with free-slip cells or ghost cells without a handler (LBM_ERR_STATE). */
+int lbm_adjoint_forward(lbm_domain* d, int64_t nsteps, int64_t ckpt_every);
+
+/* J = sum over the interior fluid cells of box = {x0, xE, y0, yE, z0, zE} (inclusive, interior
+ * coordinates) of rho |u|^2 / 2, from the current post-collision populations, FP64. */
+int lbm_adjoint_objective_ke(lbm_domain* d, const int64_t box[6], double* J);
+
+/* dJ/dtheta of the objective of box at the end of the last lbm_adjoint_forward, times dJ (the
+ * upstream gradient when wrapped in an autodiff framework), with the state the run started from
+ * held fixed. That state includes the boundary values its first step pulls (computed by the step
+ * before it, as in the reference), so theta acts through the run's steps 2 .. n. Recomputes each
+ * checkpoint segment
+ * while recording per-cell mass and momentum, then runs the adjoint steps backwards through it.
+ * grad_inflow (may be NULL): 3 doubles per cell over all cells (reference cell order), the
+ * gradient with respect to the inflow velocity of each inflow cell (the per-cell profile or the
+ * handler's uniform velocity at that cell); grad_wall (may be NULL): 3 doubles per handler id
+ * (1-based id h at index 3*(h-1)), the gradient with respect to each moving wall's velocity. The
+ * state is left as lbm_adjoint_forward left it. */
+int lbm_adjoint_backward(lbm_domain* d, const int64_t box[6], double dJ, double* grad_inflow,
+                         double* grad_wall);
+
 /* Blocks until all work queued on the handle's stream has finished. */
 int lbm_sync(lbm_domain* d);
 

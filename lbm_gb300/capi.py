@@ -58,6 +58,9 @@ SIGNATURES = {
     "lbm_moments": (ctypes.c_int, [_P, _P, _P]),
     "lbm_moments_noalloc": (ctypes.c_int, [_P, _P, _P]),
     "lbm_reduce_mass_momentum": (ctypes.c_int, [_P, _P]),
+    "lbm_adjoint_forward": (ctypes.c_int, [_P, _I64, _I64]),
+    "lbm_adjoint_objective_ke": (ctypes.c_int, [_P, _P, _P]),
+    "lbm_adjoint_backward": (ctypes.c_int, [_P, _P, _D, _P, _P]),
     "lbm_sync": (ctypes.c_int, [_P]),
     "lbm_get_stream": (ctypes.c_int, [_P, ctypes.POINTER(_P)]),
     "lbm_steps_done": (_I64, [_P]),

@@ -1,0 +1,295 @@
+// Discrete adjoint of the time step (an extension: the reference has no gradients).
+//
+// Forward step t (cell x, direction q): the pulled population g_t,q(x) is the neighbour's
+// post-collision f*_{t-1,q}(x - c_q), or, when x - c_q is a boundary cell, that cell's handler
+// value B_q(f*_{t-1}(x), theta) (theta: wall or inflow velocity), evaluated at the end of step
+// t-1; f*_t(x) = BGK(g_t(x)). The boundary values that the first step of a run pulls belong to the
+// state the run starts from (the initial values at step 1: the reference runs no handler before its
+// first stream), so over steps s0+1 .. s0+n theta enters through steps s0+2 .. s0+n.
+//
+// With lambda_t = dJ/df*_t and mu_t = dJ/dg_t the adjoint step is, per fluid cell x,
+//   lambda_{t-1}(x)_p = mu_t(x + c_p)_p                    (x + c_p fluid; the transposed pull)
+//                     + sum_{q: x - c_q boundary} mu_t(x)_q dB_q/df*_p      (t >= 2)
+//   mu_{t-1}(x)       = J_BGK(g_{t-1}(x))^T lambda_{t-1}(x)
+// and dJ/dtheta += sum_{t >= s0+2} sum_{x, q} mu_t(x)_q dB_q/dtheta. The BGK Jacobian depends on
+// g only through its mass and momentum, which the recompute segments record per cell (the same
+// as the post-collision ones: BGK conserves them), so the adjoint reads 4 values per cell and
+// step besides the Q adjoint populations.
+#pragma once
+
+#include "kernels.cuh"
+
+namespace lbmg {
+
+template <class T>
+struct AdjParams {
+    const uint8_t* flag;
+    const uint32_t* link;
+    const BcEntry* bc;
+    const double* profile;
+    Geom g;
+    T omega;
+    const T* mu_in;       // mu_t, Q planes of PS
+    T* mu_out;            // mu_{t-1}
+    const T* rec;         // mass and momentum of g_{t-1}, 4 per cell (layout index)
+    int bc_terms;         // 1: the handler terms of step t apply (t >= s0 + 2)
+    int write_mu;         // 0: only the theta gradients of step t
+    double* grad_inflow;  // 3 per cell, reference cell order (inflow cells)
+    double* grad_wall;    // 3 per handler
+};
+
+template <class T>
+struct AdjConst;
+template <>
+struct AdjConst<float> {
+    static constexpr float A = kA, B = kB, C = kC;
+};
+template <>
+struct AdjConst<double> {
+    static constexpr double A = 1.0 / kCS2, B = 1.0 / kCS4x2, C = 1.0 / kCS2x2;
+};
+
+// In place: lam <- J^T lam for the BGK map at a state of mass rho and momentum j:
+//   J = (1 - omega) I + omega d feq / dg,  feq_q = w_q rho (1 + A cu + B cu^2 - C uu)
+template <class L, class T>
+__device__ __forceinline__ void bgk_adjoint(T (&lam)[L::Q], T rho, T jx, T jy, T jz, T omega)
+{
+    using K = AdjConst<T>;
+    const T ir = T(1) / rho;
+    const T ux = jx * ir, uy = jy * ir, uz = jz * ir;
+    const T uu = ux * ux + uy * uy + uz * uz;
+    T s0 = 0, vx = 0, vy = 0, vz = 0;
+#pragma unroll
+    for (int q = 0; q < L::Q; ++q) {
+        const T cx = T(L::c(q, 0)), cy = T(L::c(q, 1)), cz = T(L::c(q, 2));
+        const T cu = cx * ux + cy * uy + cz * uz;
+        const T w = T(L::w(q));
+        const T lw = lam[q] * w;
+        s0 += lw * (T(1) + K::A * cu + K::B * cu * cu - K::C * uu);
+        const T g = lw * rho;
+        const T k1 = K::A + T(2) * K::B * cu;
+        vx += g * (k1 * cx - T(2) * K::C * ux);
+        vy += g * (k1 * cy - T(2) * K::C * uy);
+        vz += g * (k1 * cz - T(2) * K::C * uz);
+    }
+    const T om1 = T(1) - omega;
+#pragma unroll
+    for (int p = 0; p < L::Q; ++p) {
+        const T dx = T(L::c(p, 0)) - ux, dy = T(L::c(p, 1)) - uy, dz = T(L::c(p, 2)) - uz;
+        lam[p] = om1 * lam[p] + omega * (s0 + (dx * vx + dy * vy + dz * vz) * ir);
+    }
+}
+
+// d feq_q / d u_d at (rho0, u), for the handler terms.
+template <class L, class T>
+__device__ __forceinline__ T dfeq_du(int q, int d, T rho0, T cu, T ud)
+{
+    using K = AdjConst<T>;
+    return T(rt_w<L>(q)) * rho0 * ((K::A + T(2) * K::B * cu) * T(rt_c<L>(q, d)) - T(2) * K::C * ud);
+}
+
+// Sums each moving-wall handler's gradient over the warp and adds it with one atomic per handler
+// and warp (the lid of a cavity would otherwise send every link's atomics to the same three
+// addresses). Every lane of the warp must call it.
+__device__ __forceinline__ void warp_flush_wall(double* grad_wall, int hid, const double (&gw)[3])
+{
+    const unsigned full = 0xffffffffu;
+    const int lane = static_cast<int>(threadIdx.x & 31);
+    int mine = hid;
+    for (;;) {
+        const unsigned pending = __ballot_sync(full, mine >= 0);
+        if (!pending) break;
+        const int leader = __ffs(pending) - 1;
+        const int target = __shfl_sync(full, mine, leader);
+        double v[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) v[k] = mine == target ? gw[k] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) v[k] += __shfl_xor_sync(full, v[k], o);
+        if (lane == leader)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) atomicAdd(grad_wall + 3 * target + k, v[k]);
+        if (mine == target) mine = -1;
+    }
+}
+
+template <class L, class T>
+__global__ void __launch_bounds__(kBlockX) adjoint_step_kernel(const AdjParams<T> A)
+{
+    using K = AdjConst<T>;
+    constexpr int Q = L::Q;
+    const int x = 1 + static_cast<int>(blockIdx.x) * kBlockX + static_cast<int>(threadIdx.x);
+    const int y = 1 + static_cast<int>(blockIdx.y), z = 1 + static_cast<int>(blockIdx.z);
+    const int i = cidx(A.g, x, y, z);
+    const uint8_t fl = x <= A.g.xl ? A.flag[i] : static_cast<uint8_t>(0xff);
+    const bool active = is_fluid(fl);
+    int wall_h = -1;               // moving-wall handler whose gradient this thread accumulates
+    double gw[3] = {0.0, 0.0, 0.0};
+    if (active) {
+        const size_t PS = A.g.PS;
+        T lam[Q];
+        // transposed pull: x's f*_p became the pulled g_p of x + c_p
+#pragma unroll
+        for (int p = 0; p < Q; ++p) {
+            int mx, my, mz;
+            nbr_xyz(A.g, x, y, z, L::c(p, 0), L::c(p, 1), L::c(p, 2), mx, my, mz);
+            const int m = cidx(A.g, mx, my, mz);
+            lam[p] = is_fluid(A.flag[m]) ? A.mu_in[static_cast<size_t>(p) * PS + m] : T(0);
+        }
+        const T rho_s = A.rec[4 * static_cast<size_t>(i) + 0];
+        const T jxs = A.rec[4 * static_cast<size_t>(i) + 1];
+        const T jys = A.rec[4 * static_cast<size_t>(i) + 2];
+        const T jzs = A.rec[4 * static_cast<size_t>(i) + 3];
+        const uint32_t link = fl == kFluidEdge ? A.link[i] : 0u;
+        if (A.bc_terms && link) {
+            T spread = 0;              // added to every direction (handlers that use sum f*)
+            T sx = 0, sy = 0, sz = 0;  // outflow / pressure: added as c_p . s
+#pragma unroll
+            for (int q = 0; q < Q; ++q) {
+                if (!((link >> q) & 1u)) continue;
+                int bx, by, bz;
+                nbr_xyz(A.g, x, y, z, -L::c(q, 0), -L::c(q, 1), -L::c(q, 2), bx, by, bz);
+                const uint8_t flb = A.flag[cidx(A.g, bx, by, bz)];
+                if (flb < kFirstHandler) continue;
+                const int h = flb - kFirstHandler;
+                const BcEntry& be = A.bc[h];
+                const T mu_q = A.mu_in[static_cast<size_t>(q) * PS + i];
+                const int qb = L::Q - 1 - q;
+                switch (be.type) {
+                case kNoSlip:  // B_q = f*_qb
+                    lam[qb] += mu_q;
+                    break;
+                case kMovingWall: {  // B_q = f*_qb + 2 w_q rho* (c_q . u_w) / cs2
+                    const T cuw = T(L::c(q, 0)) * T(be.v[0]) + T(L::c(q, 1)) * T(be.v[1]) +
+                                  T(L::c(q, 2)) * T(be.v[2]);
+                    lam[qb] += mu_q;
+                    spread += mu_q * T(2) * T(L::w(q)) * cuw * K::A;
+                    const double gcoef = static_cast<double>(mu_q * T(2) * T(L::w(q)) * rho_s * K::A);
+                    if (wall_h < 0) wall_h = h;
+                    if (h == wall_h) {
+                        gw[0] += gcoef * L::c(q, 0);
+                        gw[1] += gcoef * L::c(q, 1);
+                        gw[2] += gcoef * L::c(q, 2);
+                    } else {
+                        atomicAdd(A.grad_wall + 3 * h + 0, gcoef * L::c(q, 0));
+                        atomicAdd(A.grad_wall + 3 * h + 1, gcoef * L::c(q, 1));
+                        atomicAdd(A.grad_wall + 3 * h + 2, gcoef * L::c(q, 2));
+                    }
+                    break;
+                }
+                case kInflow: {  // B_q = feq_q(rho0, u_in)
+                    const size_t r = ref_idx(A.g, bx, by, bz);
+                    const double* v = be.has_profile ? A.profile + 3 * r : be.v;
+                    const T vx = T(v[0]), vy = T(v[1]), vz = T(v[2]);
+                    const T cu = T(L::c(q, 0)) * vx + T(L::c(q, 1)) * vy + T(L::c(q, 2)) * vz;
+                    const T r0 = T(be.rho);
+                    atomicAdd(A.grad_inflow + 3 * r + 0, static_cast<double>(mu_q * dfeq_du<L, T>(q, 0, r0, cu, vx)));
+                    atomicAdd(A.grad_inflow + 3 * r + 1, static_cast<double>(mu_q * dfeq_du<L, T>(q, 1, r0, cu, vy)));
+                    atomicAdd(A.grad_inflow + 3 * r + 2, static_cast<double>(mu_q * dfeq_du<L, T>(q, 2, r0, cu, vz)));
+                    break;
+                }
+                case kOutflow:
+                case kPressure: {
+                    // B_q = feq_q(r0, u) + feq_qb(r0, u) - f*_qb with u = j*/r0:
+                    // dB_q/df*_p = (D . c_p)/r0 - delta(p, qb), D_d = w_q r0 (4 B cu c_qd - 4 C u_d)
+                    const T r0 = T(be.rho);
+                    const T ux = jxs / r0, uy = jys / r0, uz = jzs / r0;
+                    const T cu = T(L::c(q, 0)) * ux + T(L::c(q, 1)) * uy + T(L::c(q, 2)) * uz;
+                    const T wr = T(L::w(q)) * r0;
+                    const T dx = wr * (T(4) * K::B * cu * T(L::c(q, 0)) - T(4) * K::C * ux);
+                    const T dy = wr * (T(4) * K::B * cu * T(L::c(q, 1)) - T(4) * K::C * uy);
+                    const T dz = wr * (T(4) * K::B * cu * T(L::c(q, 2)) - T(4) * K::C * uz);
+                    lam[qb] -= mu_q;
+                    sx += mu_q * dx / r0;
+                    sy += mu_q * dy / r0;
+                    sz += mu_q * dz / r0;
+                    break;
+                }
+                default:
+                    break;
+                }
+            }
+#pragma unroll
+            for (int p = 0; p < Q; ++p)
+                lam[p] += spread + T(L::c(p, 0)) * sx + T(L::c(p, 1)) * sy + T(L::c(p, 2)) * sz;
+        }
+        if (A.write_mu) {
+            bgk_adjoint<L, T>(lam, rho_s, jxs, jys, jzs, A.omega);
+#pragma unroll
+            for (int p = 0; p < Q; ++p) A.mu_out[static_cast<size_t>(p) * PS + i] = lam[p];
+        }
+    }
+    if (A.bc_terms) warp_flush_wall(A.grad_wall, wall_h, gw);
+}
+
+// mu_T = J^T lambda_T with lambda_T = dJ/df*_T of J = sum_{x in box} rho |u|^2 / 2, i.e.
+// lambda_T(x)_p = u . c_p - |u|^2 / 2 inside the box (u of the final state), 0 outside.
+template <class L, class T>
+__global__ void __launch_bounds__(kBlockX)
+    adjoint_terminal_kernel(const uint8_t* flag, Geom g, T omega, const T* rec, Box box, T* mu_out)
+{
+    constexpr int Q = L::Q;
+    const int x = 1 + static_cast<int>(blockIdx.x) * kBlockX + static_cast<int>(threadIdx.x);
+    if (x > g.xl) return;
+    const int y = 1 + static_cast<int>(blockIdx.y), z = 1 + static_cast<int>(blockIdx.z);
+    const int i = cidx(g, x, y, z);
+    if (!is_fluid(flag[i])) return;
+    const T rho = rec[4 * static_cast<size_t>(i)];
+    const T jx = rec[4 * static_cast<size_t>(i) + 1], jy = rec[4 * static_cast<size_t>(i) + 2],
+            jz = rec[4 * static_cast<size_t>(i) + 3];
+    const bool in = x >= box.x0 && x <= box.x1 && y >= box.y0 && y <= box.y1 && z >= box.z0 && z <= box.z1;
+    const T ux = jx / rho, uy = jy / rho, uz = jz / rho;
+    const T half_uu = T(0.5) * (ux * ux + uy * uy + uz * uz);
+    T lam[Q];
+#pragma unroll
+    for (int p = 0; p < Q; ++p)
+        lam[p] = in ? T(L::c(p, 0)) * ux + T(L::c(p, 1)) * uy + T(L::c(p, 2)) * uz - half_uu : T(0);
+    bgk_adjoint<L, T>(lam, rho, jx, jy, jz, omega);
+#pragma unroll
+    for (int p = 0; p < Q; ++p) mu_out[static_cast<size_t>(p) * g.PS + i] = lam[p];
+}
+
+// Kinetic energy sum_{x in box, fluid} rho |u|^2 / 2 of the post-collision state, FP64; one
+// partial per block (fixed grid), summed in order by reduce_final_kernel.
+template <class L, class S>
+__global__ void __launch_bounds__(kReduceThreads)
+    objective_ke_kernel(const S* pop, const uint8_t* flag, Geom g, int odd, Box box, double* partials)
+{
+    double acc = 0.0;
+    const int bx = box.x1 - box.x0 + 1, by = box.y1 - box.y0 + 1, bz = box.z1 - box.z0 + 1;
+    const size_t n = static_cast<size_t>(bx) * by * bz;
+    for (size_t k = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; k < n;
+         k += static_cast<size_t>(gridDim.x) * blockDim.x) {
+        const int x = box.x0 + static_cast<int>(k % bx);
+        const int y = box.y0 + static_cast<int>((k / bx) % by);
+        const int z = box.z0 + static_cast<int>(k / (static_cast<size_t>(bx) * by));
+        const int i = cidx(g, x, y, z);
+        if (!is_fluid(flag[i])) continue;
+        double m[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+        for (int p = 0; p < L::Q; ++p) {
+            const double f = to_f64<L, S>(load_post<L, S>(pop, flag, g, x, y, z, i, p, odd != 0), p);
+            m[0] += f;
+            m[1] += L::c(p, 0) * f;
+            m[2] += L::c(p, 1) * f;
+            m[3] += L::c(p, 2) * f;
+        }
+        acc += 0.5 * (m[1] * m[1] + m[2] * m[2] + m[3] * m[3]) / m[0];
+    }
+    __shared__ double red[kReduceThreads / 32];
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double v = 0.0;
+        for (int w = 0; w < kReduceThreads / 32; ++w) v += red[w];
+        partials[4 * blockIdx.x] = v;
+        partials[4 * blockIdx.x + 1] = 0.0;
+        partials[4 * blockIdx.x + 2] = 0.0;
+        partials[4 * blockIdx.x + 3] = 0.0;
+    }
+}
+
+}  // namespace lbmg

@@ -11,6 +11,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <memory>
 #include <mutex>
 #include <new>
 #include <stdexcept>
@@ -104,8 +105,18 @@ struct DevBuf {
 
 }  // namespace
 
+// Checkpoints of a gradient run (lbm_adjoint_forward .. lbm_adjoint_backward).
+struct AdjointRun {
+    bool ready = false;
+    long long s0 = 0;  // steps done when the run started
+    long long n = 0;   // steps of the run
+    long long k = 0;   // steps between checkpoints
+    std::vector<std::unique_ptr<DevBuf<unsigned char>>> ckpt;  // state after s0 + j*k steps
+};
+
 struct lbm_domain {
     DomainDev dev{};
+    AdjointRun adj;
     const KernelOps* ops = nullptr;
     cudaStream_t stream = nullptr;
     int Q = 0;
@@ -347,6 +358,7 @@ void lbm_domain::build_side_lists()
 void lbm_domain::finalize()
 {
     if (!geom_dirty) return;
+    adj.ready = false;
     const Geom& g = dev.g;
     DevBuf<double> carry;
     if (state_custom) {
@@ -643,6 +655,7 @@ int lbm_set_populations(lbm_domain* d, const double* f)
         check(cudaMemcpyAsync(tmp.p, f, tmp.bytes(), cudaMemcpyHostToDevice, d->stream), "upload populations");
         d->ops->scatter(d->dev, d->steps, tmp.p, d->stream);
         check(cudaGetLastError(), "scatter kernel");
+        d->adj.ready = false;
         check(cudaStreamSynchronize(d->stream), "set populations");
         d->state_custom = true;
     });
@@ -668,7 +681,8 @@ int lbm_step(lbm_domain* d, int64_t nsteps)
     return guarded(d, [&] {
         if (nsteps < 0) throw ArgError("nsteps must be >= 0");
         d->finalize();
-        for (int64_t k = 0; k < nsteps; ++k) d->ops->step(d->dev, d->steps + 1 + k, nullptr, d->stream);
+        for (int64_t k = 0; k < nsteps; ++k) d->ops->step(d->dev, d->steps + 1 + k, nullptr, nullptr, d->stream);
+        if (nsteps > 0) d->adj.ready = false;
         check(cudaGetLastError(), "step kernel launch");
         d->steps += nsteps;
         if (nsteps > 0) d->state_custom = true;
@@ -683,13 +697,14 @@ int lbm_step_monitored(lbm_domain* d, int64_t nsteps, double* totals)
         d->finalize();
         for (int64_t k = 0; k < nsteps; ++k) {
             double* slot = d->mon_ring.p + 4 * (k % kMonRing);
-            d->ops->step(d->dev, d->steps + 1 + k, slot, d->stream);
+            d->ops->step(d->dev, d->steps + 1 + k, slot, nullptr, d->stream);
             check(cudaMemcpyAsync(totals + 4 * k, slot, 4 * sizeof(double), cudaMemcpyDeviceToHost, d->stream),
                   "copy step totals");
         }
         check(cudaGetLastError(), "step kernel launch");
         d->steps += nsteps;
         if (nsteps > 0) d->state_custom = true;
+        if (nsteps > 0) d->adj.ready = false;
     });
 }
 
@@ -796,6 +811,135 @@ int lbm_memory_info(const lbm_domain* d, uint64_t* device_bytes, uint64_t* step_
         if (fluid_cells) *fluid_cells = m->fluid_cells;
         if (launches_per_step)
             *launches_per_step = 1 + (m->dev.n_gf > 0) + (m->dev.n_fs > 0);
+    });
+}
+
+namespace {
+
+Box to_box(const lbm_domain* d, const int64_t box[6])
+{
+    if (!box) throw ArgError("box is NULL");
+    const Geom& g = d->dev.g;
+    if (!(box[0] >= 1 && box[0] <= box[1] && box[1] <= g.xl && box[2] >= 1 && box[2] <= box[3] &&
+          box[3] <= g.yl && box[4] >= 1 && box[4] <= box[5] && box[5] <= g.zl))
+        throw ArgError("objective box must be a non-empty box of interior cells");
+    return Box{static_cast<int>(box[0]), static_cast<int>(box[1]), static_cast<int>(box[2]),
+               static_cast<int>(box[3]), static_cast<int>(box[4]), static_cast<int>(box[5])};
+}
+
+}  // namespace
+
+int lbm_adjoint_forward(lbm_domain* d, int64_t nsteps, int64_t ckpt_every)
+{
+    return guarded(d, [&] {
+        if (nsteps < 1 || ckpt_every < 1) throw ArgError("nsteps and ckpt_every must be >= 1");
+        d->finalize();
+        if (d->dev.n_fs > 0 || d->dev.n_gf > 0)
+            throw StateError("gradients are not available with free-slip cells or ghost cells without a handler");
+        AdjointRun& a = d->adj;
+        a.ready = false;
+        a.ckpt.clear();
+        a.s0 = d->steps;
+        a.n = nsteps;
+        a.k = ckpt_every;
+        const long long nseg = (nsteps + ckpt_every - 1) / ckpt_every;
+        for (long long j = 0; j < nseg; ++j) {
+            a.ckpt.emplace_back(new DevBuf<unsigned char>());
+            a.ckpt.back()->alloc(d->pop.bytes(), "cudaMalloc(checkpoint)");
+        }
+        for (long long j = 0; j < nseg; ++j) {
+            check(cudaMemcpyAsync(a.ckpt[j]->p, d->pop.p, d->pop.bytes(), cudaMemcpyDeviceToDevice, d->stream),
+                  "store checkpoint");
+            const long long len = std::min<long long>(ckpt_every, nsteps - j * ckpt_every);
+            for (long long r = 0; r < len; ++r) d->ops->step(d->dev, d->steps + 1 + r, nullptr, nullptr, d->stream);
+            d->steps += len;
+        }
+        check(cudaGetLastError(), "step kernel launch");
+        d->state_custom = true;
+        a.ready = true;
+    });
+}
+
+int lbm_adjoint_objective_ke(lbm_domain* d, const int64_t box[6], double* J)
+{
+    return guarded(d, [&] {
+        if (!J) throw ArgError("J is NULL");
+        d->finalize();
+        const Box b = to_box(d, box);
+        double* partials = d->red.p;
+        double* total = d->red.p + 4 * kReduceBlocks;
+        d->ops->objective_ke(d->dev, d->steps, b, partials, kReduceBlocks, total, d->stream);
+        check(cudaGetLastError(), "objective kernel");
+        check(cudaMemcpyAsync(J, total, sizeof(double), cudaMemcpyDeviceToHost, d->stream), "download objective");
+        check(cudaStreamSynchronize(d->stream), "objective");
+        d->check_device_error();
+    });
+}
+
+int lbm_adjoint_backward(lbm_domain* d, const int64_t box[6], double dJ, double* grad_inflow, double* grad_wall)
+{
+    return guarded(d, [&] {
+        AdjointRun& a = d->adj;
+        if (!a.ready || d->steps != a.s0 + a.n || d->geom_dirty)
+            throw StateError("lbm_adjoint_backward needs the state lbm_adjoint_forward left (no steps, "
+                             "population writes or geometry changes in between)");
+        const Box b = to_box(d, box);
+        const size_t PS = d->dev.g.PS;
+        const size_t Tb = d->ops->compute_bytes;
+        const size_t rec_bytes = 4 * PS * Tb;
+        DevBuf<unsigned char> mu[2], rec, backup;
+        DevBuf<double> gin, gwall;
+        mu[0].alloc(static_cast<size_t>(d->Q) * PS * Tb, "cudaMalloc(adjoint populations)");
+        mu[1].alloc(static_cast<size_t>(d->Q) * PS * Tb, "cudaMalloc(adjoint populations)");
+        rec.alloc(static_cast<size_t>(a.k) * rec_bytes, "cudaMalloc(recompute record)");
+        backup.alloc(d->pop.bytes(), "cudaMalloc(state backup)");
+        gin.alloc(3 * d->ng, "cudaMalloc(inflow gradient)");
+        gwall.alloc(3 * kMaxHandlers, "cudaMalloc(wall gradient)");
+        check(cudaMemsetAsync(gin.p, 0, gin.bytes(), d->stream), "clear gradient");
+        check(cudaMemsetAsync(gwall.p, 0, gwall.bytes(), d->stream), "clear gradient");
+        check(cudaMemsetAsync(mu[0].p, 0, mu[0].bytes(), d->stream), "clear adjoint");
+        check(cudaMemsetAsync(mu[1].p, 0, mu[1].bytes(), d->stream), "clear adjoint");
+        check(cudaMemcpyAsync(backup.p, d->pop.p, d->pop.bytes(), cudaMemcpyDeviceToDevice, d->stream), "state backup");
+
+        const long long nseg = static_cast<long long>(a.ckpt.size());
+        int cur = 0;
+        long long t_cur = 0;  // mu[cur] holds mu_{t_cur}
+        for (long long j = nseg - 1; j >= 0; --j) {
+            const long long c = a.s0 + j * a.k;
+            const long long len = std::min<long long>(a.k, a.n - j * a.k);
+            check(cudaMemcpyAsync(d->pop.p, a.ckpt[j]->p, d->pop.bytes(), cudaMemcpyDeviceToDevice, d->stream),
+                  "restore checkpoint");
+            for (long long r = 1; r <= len; ++r)  // recompute, recording rec_{c+r}
+                d->ops->step(d->dev, c + r, nullptr, rec.p + (r - 1) * rec_bytes, d->stream);
+            if (j == nseg - 1) {
+                d->ops->adj_terminal(d->dev, rec.p + (len - 1) * rec_bytes, mu[cur].p, b, d->stream);
+                t_cur = c + len;
+            }
+            // mu_t -> mu_{t-1} with the record of step t-1; the run's first step (t = s0 + 1) pulls
+            // the boundary values the starting state holds, so the loop ends at t = s0 + 2
+            for (long long t = t_cur; t >= c + 2; --t) {
+                d->ops->adj_step(d->dev, mu[cur].p, mu[1 - cur].p, rec.p + (t - c - 2) * rec_bytes, 1, 1, gin.p,
+                                 gwall.p, d->stream);
+                cur = 1 - cur;
+                t_cur = t - 1;
+            }
+        }
+        check(cudaMemcpyAsync(d->pop.p, backup.p, d->pop.bytes(), cudaMemcpyDeviceToDevice, d->stream), "restore state");
+        check(cudaGetLastError(), "adjoint kernels");
+        if (grad_inflow) {
+            check(cudaMemcpyAsync(grad_inflow, gin.p, gin.bytes(), cudaMemcpyDeviceToHost, d->stream),
+                  "download inflow gradient");
+        }
+        std::vector<double> hw(3 * kMaxHandlers);
+        check(cudaMemcpyAsync(hw.data(), gwall.p, gwall.bytes(), cudaMemcpyDeviceToHost, d->stream),
+              "download wall gradient");
+        check(cudaStreamSynchronize(d->stream), "adjoint");
+        d->check_device_error();
+        if (grad_inflow)
+            for (size_t k = 0; k < 3 * d->ng; ++k) grad_inflow[k] *= dJ;
+        if (grad_wall)
+            for (size_t h = 0; h < d->bcs.size(); ++h)
+                for (int k = 0; k < 3; ++k) grad_wall[3 * h + k] = dJ * hw[3 * h + k];
     });
 }
 

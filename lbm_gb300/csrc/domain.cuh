@@ -55,6 +55,11 @@ struct BcEntry {
     double rho;       // rho-ref (inflow, outflow) or rho-in (pressure)
 };
 
+// An inclusive box of interior cells (the objective region of the adjoint).
+struct Box {
+    int x0, x1, y0, y1, z0, z1;
+};
+
 struct Geom {
     int xl, yl, zl;
     int XS, YS, ZS;  // row stride (elements), rows per plane slice (yl+2), slices (zl+2)

@@ -343,6 +343,8 @@ struct StepParams {
     int* err;              // set to 1 when a bounded wait gives up
     double* mon;           // kMonBuckets x 4 FP64 accumulators of the step's mass and momentum,
                            // or nullptr
+    typename Store<S>::C* rec;  // per cell (layout index i): rec[4i..4i+3] = mass and momentum of
+                                // the populations the cell pulled this step, or nullptr
     Geom g;
     double tau;
     float omega;
@@ -356,6 +358,17 @@ __device__ __forceinline__ void collide_any(typename Store<S>::C (&f)[L::Q], con
         collide_shifted<L>(f, P.omega, m);
     else
         collide_exact<L>(f, P.tau, m);
+}
+
+// Stores a cell's pre-collision mass and momentum for the adjoint's recompute segments.
+template <class S>
+__device__ __forceinline__ void record_moments(typename Store<S>::C* rec, int i, const double (&m)[4])
+{
+    using T = typename Store<S>::C;
+    rec[4 * static_cast<size_t>(i) + 0] = static_cast<T>(m[0]);
+    rec[4 * static_cast<size_t>(i) + 1] = static_cast<T>(m[1]);
+    rec[4 * static_cast<size_t>(i) + 2] = static_cast<T>(m[2]);
+    rec[4 * static_cast<size_t>(i) + 3] = static_cast<T>(m[3]);
 }
 
 // Adds the warp's totals of m to one accumulator bucket. Every lane of the warp must call it.
@@ -516,6 +529,7 @@ __device__ __forceinline__ void edge_block(const StepParams<S>& P, int blk, unsi
             }
         }
         collide_any<L, S>(f, P, m);
+        if (P.rec) record_moments<S>(P.rec, i, m);
         store_edge_populations<L, S, ODD>(P, x, y, z, i, link, f);
         if (link & ((1u << Q) - 1u)) {
             T* fs = reinterpret_cast<T*>(smem_raw) + tx;
@@ -599,6 +613,7 @@ __device__ __forceinline__ void row_block(const StepParams<S>& P, int rb, int ns
 #pragma unroll
             for (int q = 0; q < Q; ++q) f[q] = St::ld(buf + q * W + PAD + tx - (ODD ? L::c(q, 0) : 0));
             collide_any<L, S>(f, P, m);
+            if (P.rec) record_moments<S>(P.rec, i, m);
 #pragma unroll
             for (int p = 0; p < Q; ++p) {
                 if (ODD) {

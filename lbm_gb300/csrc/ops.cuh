@@ -15,8 +15,9 @@ struct KernelOps {
     // fluid cells -> kFluidBulk / kFluidEdge
     void (*classify)(const DomainDev& d, cudaStream_t s);
     // one time step number `t` (1-based): fused kernel, then the side passes; with mon_out
-    // (device, 4 doubles) also the FP64 mass and momentum the step started from
-    void (*step)(const DomainDev& d, long long t, double* mon_out, cudaStream_t s);
+    // (device, 4 doubles) also the FP64 mass and momentum the step started from; with rec
+    // (device, 4 compute-type values per cell) each cell's pre-collision mass and momentum
+    void (*step)(const DomainDev& d, long long t, double* mon_out, void* rec, cudaStream_t s);
     // state after `k` steps -> AoS FP64 over all cells (device buffer)
     void (*gather)(const DomainDev& d, long long k, double* out, cudaStream_t s);
     // AoS FP64 over all cells (device buffer) -> state after `k` steps
@@ -26,6 +27,16 @@ struct KernelOps {
     // FP64 totals into out[4] (device), partials: scratch of 4 * reduce_blocks doubles
     void (*reduce)(const DomainDev& d, long long k, double* partials, int reduce_blocks,
                    double* out, cudaStream_t s);
+    // adjoint (compute type: double for FP64 storage, float otherwise)
+    size_t compute_bytes;
+    // mu_T from the final step's record and the objective box
+    void (*adj_terminal)(const DomainDev& d, const void* rec, void* mu_out, Box box, cudaStream_t s);
+    // mu_t -> mu_{t-1} with the record of step t-1; theta gradients of step t
+    void (*adj_step)(const DomainDev& d, const void* mu_in, void* mu_out, const void* rec, int bc_terms,
+                     int write_mu, double* grad_inflow, double* grad_wall, cudaStream_t s);
+    // kinetic energy of the box into out[0] (device), partials as for reduce
+    void (*objective_ke)(const DomainDev& d, long long k, Box box, double* partials, int reduce_blocks,
+                         double* out, cudaStream_t s);
 };
 
 const KernelOps* ops_fp64(int q);

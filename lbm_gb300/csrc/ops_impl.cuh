@@ -4,6 +4,7 @@
 
 #include "ops.cuh"
 #include "state_kernels.cuh"
+#include "adjoint.cuh"
 
 namespace lbmg {
 namespace {
@@ -34,6 +35,7 @@ StepParams<S> step_params(const DomainDev& d)
     p.g = d.g;
     p.err = d.err;
     p.mon = nullptr;
+    p.rec = nullptr;
     p.tau = d.tau;
     p.omega = static_cast<float>(1.0 / d.tau);
     return p;
@@ -65,10 +67,11 @@ struct Launch {
                 pop, d.flag, d.g, d.fs_link, d.n_fs, copy, d.gf_pop, d.n_gf, copy);
     }
 
-    static void step(const DomainDev& d, long long t, double* mon_out, cudaStream_t s)
+    static void step(const DomainDev& d, long long t, double* mon_out, void* rec, cudaStream_t s)
     {
         StepParams<S> p = step_params<L, S>(d);
         p.mon = mon_out ? d.mon : nullptr;
+        p.rec = static_cast<typename Store<S>::C*>(rec);
         const int nseg_x = (d.g.xl + kRowCells - 1) / kRowCells;
         const int nseg = nseg_x * d.g.yl * d.g.zl;
         const int row_blocks = (nseg + kSegs - 1) / kSegs;
@@ -133,9 +136,46 @@ struct Launch {
         reduce_final_kernel<<<1, 32, 0, s>>>(partials, nblocks, out);
     }
 
+    using T = typename Store<S>::C;
+
+    static void adj_terminal(const DomainDev& d, const void* rec, void* mu_out, Box box, cudaStream_t s)
+    {
+        adjoint_terminal_kernel<L, T><<<cell_grid(d.g), kBlockX, 0, s>>>(
+            d.flag, d.g, static_cast<T>(1.0 / d.tau), static_cast<const T*>(rec), box, static_cast<T*>(mu_out));
+    }
+
+    static void adj_step(const DomainDev& d, const void* mu_in, void* mu_out, const void* rec, int bc_terms,
+                         int write_mu, double* grad_inflow, double* grad_wall, cudaStream_t s)
+    {
+        AdjParams<T> a;
+        a.flag = d.flag;
+        a.link = d.link;
+        a.bc = d.bc;
+        a.profile = d.profile;
+        a.g = d.g;
+        a.omega = static_cast<T>(1.0 / d.tau);
+        a.mu_in = static_cast<const T*>(mu_in);
+        a.mu_out = static_cast<T*>(mu_out);
+        a.rec = static_cast<const T*>(rec);
+        a.bc_terms = bc_terms;
+        a.write_mu = write_mu;
+        a.grad_inflow = grad_inflow;
+        a.grad_wall = grad_wall;
+        adjoint_step_kernel<L, T><<<cell_grid(d.g), kBlockX, 0, s>>>(a);
+    }
+
+    static void objective_ke(const DomainDev& d, long long k, Box box, double* partials, int nblocks,
+                             double* out, cudaStream_t s)
+    {
+        objective_ke_kernel<L, S><<<nblocks, kReduceThreads, 0, s>>>(
+            static_cast<const S*>(d.pop), d.flag, d.g, static_cast<int>(k & 1), box, partials);
+        reduce_final_kernel<<<1, 32, 0, s>>>(partials, nblocks, out);
+    }
+
     static const KernelOps* table()
     {
-        static const KernelOps t = {&init, &classify, &step, &gather, &scatter, &moments, &reduce};
+        static const KernelOps t = {&init,    &classify, &step,      &gather,       &scatter,  &moments,
+                                    &reduce,  sizeof(T), &adj_terminal, &adj_step, &objective_ke};
         return &t;
     }
 };

@@ -202,6 +202,7 @@ class Domain:
             raise LbmError(capi.LBM_ERR_ARG, "mask size must be xl*yl*zl")
         h = ctypes.c_int()
         check(self._lib.lbm_set_solid_mask(self._h, m.ctypes.data, ctypes.byref(h)), self._h)
+        self._handlers.append(h.value)
         return h.value
 
     def set_periodic(self, px: bool, py: bool, pz: bool) -> None:
@@ -283,6 +284,28 @@ class Domain:
         out = np.empty(4, dtype=np.float64)
         check(self._lib.lbm_reduce_mass_momentum(self._h, out.ctypes.data), self._h)
         return out
+
+    # -- gradients (extension) -------------------------------------------------------------
+    def adjoint_forward(self, nsteps: int, ckpt_every: int) -> None:
+        """nsteps steps from the current state, checkpointing every ckpt_every steps."""
+        check(self._lib.lbm_adjoint_forward(self._h, int(nsteps), int(ckpt_every)), self._h)
+
+    def objective_ke(self, box) -> float:
+        """sum over the fluid cells of box (x0, xE, y0, yE, z0, zE) of rho |u|^2 / 2."""
+        b = (ctypes.c_int64 * 6)(*box)
+        j = ctypes.c_double()
+        check(self._lib.lbm_adjoint_objective_ke(self._h, b, ctypes.byref(j)), self._h)
+        return j.value
+
+    def adjoint_backward(self, box, dJ: float = 1.0):
+        """(grad_inflow (Ng, 3), grad_wall (handlers, 3)) of objective_ke(box) at the end of the last
+        adjoint_forward, times dJ."""
+        b = (ctypes.c_int64 * 6)(*box)
+        gin = np.zeros((self.ncells, 3), dtype=np.float64)
+        n = len(self._handlers)
+        gw = np.zeros((max(n, 1), 3), dtype=np.float64)  # row h - 1: handler id h
+        check(self._lib.lbm_adjoint_backward(self._h, b, float(dJ), gin.ctypes.data, gw.ctypes.data), self._h)
+        return gin, gw[:n]
 
     def stream_handle(self) -> int:
         s = ctypes.c_void_p()
