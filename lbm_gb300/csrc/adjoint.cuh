@@ -24,7 +24,7 @@ namespace lbmg {
 template <class T>
 struct AdjParams {
     const uint8_t* flag;
-    const uint32_t* link;
+    const uint2* link;
     const BcEntry* bc;
     const double* profile;
     Geom g;
@@ -142,7 +142,7 @@ __global__ void __launch_bounds__(kBlockX) adjoint_step_kernel(const AdjParams<T
         const T jxs = A.rec[4 * static_cast<size_t>(i) + 1];
         const T jys = A.rec[4 * static_cast<size_t>(i) + 2];
         const T jzs = A.rec[4 * static_cast<size_t>(i) + 3];
-        const uint32_t link = fl == kFluidEdge ? A.link[i] : 0u;
+        const uint32_t link = fl != kFluidBulk ? A.link[i].x : 0u;
         if (A.bc_terms && link) {
             T spread = 0;              // added to every direction (handlers that use sum f*)
             T sx = 0, sy = 0, sz = 0;  // outflow / pressure: added as c_p . s

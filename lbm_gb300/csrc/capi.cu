@@ -142,8 +142,9 @@ struct lbm_domain {
     DevBuf<double> gf_pop;
     DevBuf<int4> fs_link;
     DevBuf<double> red;  // 4 * kReduceBlocks partials + 4 totals
-    DevBuf<uint32_t> link;  // per-cell link words
+    DevBuf<uint2> link;     // per-cell link words and LinkRecord rows
     DevBuf<int> edge;       // kFluidEdge cells
+    DevBuf<LinkRecord> ltab;  // LinkRecords (shifted storage)
     DevBuf<int> errword;    // device error word, a list counter
     DevBuf<double> mon;     // step monitor accumulators
     DevBuf<double> mon_ring;  // per-step monitor results, kMonRing slots of 4 doubles
@@ -192,6 +193,7 @@ struct lbm_domain {
     void finalize();
     void build_side_lists();
     void build_edge_list();
+    void build_link_table();
     void check_device_error();
 };
 
@@ -238,6 +240,23 @@ void lbm_domain::build_edge_list()
     }
     dev.edge = edge.p;
     dev.n_edge = n;
+}
+
+void lbm_domain::build_link_table()
+{
+    int* counter = errword.p + 1;
+    int n = 0;
+    check(cudaMemsetAsync(counter, 0, sizeof(int), stream), "link record count reset");
+    ops->link_table(dev, nullptr, counter, 0, stream);
+    check(cudaMemcpyAsync(&n, counter, sizeof(int), cudaMemcpyDeviceToHost, stream), "link record count");
+    check(cudaStreamSynchronize(stream), "link record count");
+    if (n > 0) {
+        if (ltab.n < static_cast<size_t>(n)) ltab.alloc(static_cast<size_t>(n), "cudaMalloc(link records)");
+        check(cudaMemsetAsync(counter, 0, sizeof(int), stream), "link record count reset");
+        ops->link_table(dev, ltab.p, counter, n, stream);  // classify left every row at kNoRecord
+        check(cudaGetLastError(), "link record kernel");
+    }
+    dev.ltab = n > 0 ? ltab.p : nullptr;
 }
 
 void lbm_domain::check_device_error()
@@ -367,9 +386,9 @@ void lbm_domain::finalize()
         ops->gather(dev, steps, carry.p, stream);
     }
     check(cudaMemcpyAsync(flag.p, hmap.data(), hmap.size(), cudaMemcpyHostToDevice, stream), "upload flags");
-    ops->classify(dev, stream);
     check(cudaMemcpyAsync(bc.p, bcs.data(), bcs.size() * sizeof(BcEntry), cudaMemcpyHostToDevice, stream),
           "upload handler table");
+    ops->classify(dev, stream);  // reads the handler table (no-slip links)
     // merged inflow profile in reference cell order
     bool any_profile = false;
     for (const auto& p : profiles) any_profile = any_profile || !p.empty();
@@ -393,6 +412,7 @@ void lbm_domain::finalize()
     dev.profile = profile.p;
     build_side_lists();
     build_edge_list();
+    build_link_table();  // after the profile upload: inflow records hold the profile's values
     fluid_cells = 0;
     for (int z = 1; z <= g.zl; ++z)
         for (int y = 1; y <= g.yl; ++y) {

@@ -13,10 +13,12 @@
 //   link  : one 32-bit word per cell, same indexing (fluid cells only, see classify_kernel).
 //   State after k steps, in place (AA pattern): for an interior fluid cell x and direction p
 //   with neighbour m = x + c_p,
-//     k even : f*_p(x) is at plane inv(p), cell x when m is fluid; at plane p, cell m otherwise
+//     k even : f*_p(x) is at plane inv(p), cell x
 //     k odd  : f*_p(x) is at plane p, cell m
-//   and for every direction q whose upstream neighbour x - c_q is not fluid, plane q at cell x
-//   holds what that neighbour's boundary handler wrote for x (the value x pulls next step).
+//   A non-fluid cell b keeps the value its boundary handler wrote for the fluid cell n = b + c_q
+//   (the population n pulls in direction q next step) where a fluid cell would keep its own
+//   outgoing population q: k even at plane inv(q), cell b; k odd at plane q, cell n. So every
+//   cell pulls the same way from fluid and non-fluid neighbours.
 #pragma once
 
 #include <cstddef>
@@ -33,11 +35,12 @@ constexpr int kBlockX = 128;
 // Per-cell byte flag.
 enum CellFlag : uint8_t {
     kFluidBulk = 0,   // fluid; every neighbour is fluid and none wraps around a periodic axis
-    kFluidEdge = 1,   // fluid; at least one neighbour is not fluid or wraps
-    kGhostFluid = 2,  // ghost-layer cell without a boundary condition (reference: a fluid cell
+    kFluidEdge = 1,   // fluid; some neighbour wraps, or is non-fluid and not a no-slip cell
+    kFluidWall = 2,   // fluid; no neighbour wraps, some are no-slip cells, all others are fluid
+    kGhostFluid = 3,  // ghost-layer cell without a boundary condition (reference: a fluid cell
                       // that collides in place but never streams, domain.hpp:143-166), or a
                       // ghost cell of a periodic axis (never referenced)
-    kFirstHandler = 3 // kFirstHandler + h - 1 : non-fluid cell bound to handler h (1-based)
+    kFirstHandler = 4 // kFirstHandler + h - 1 : non-fluid cell bound to handler h (1-based)
 };
 constexpr int kMaxHandlers = 250;
 // Accumulator buckets of the step monitor (atomics of different warps spread over them).
@@ -67,6 +70,50 @@ struct Geom {
     size_t PS;       // plane stride (elements)
 };
 
+// Handler record of a kFluidWall cell whose links include handlers other than no-slip
+// (shifted storage only); bit q of a mask = the link from x - c_q. `spec`: every such link;
+// `wall`: moving-wall links; `inflow`: inflow links; the rest of `spec` are outflow / pressure
+// links, all with the reference density r0 (ir0 = 1 / r0). c[k], over the wall and inflow links
+// in increasing q: moving wall 2 w_q (c_q . u_w) / cs2 (added times the cell's density to the
+// bounce-back value), inflow the shifted equilibrium value itself.
+constexpr int kMaxRecordValues = 11;
+struct __align__(16) LinkRecord {
+    uint32_t spec;
+    uint32_t wall;
+    uint32_t inflow;
+    float r0;
+    float ir0;
+    float c[kMaxRecordValues];
+};
+constexpr int kLinkWords = sizeof(LinkRecord) / 4;
+constexpr uint32_t kNoRecord = 0xffffffffu;
+static_assert(sizeof(LinkRecord) == 64, "LinkRecord is 16 words");
+
+// Division of 32-bit unsigned integers by an invariant divisor d >= 1 through a multiply-high
+// (Granlund and Montgomery, "Division by invariant integers using multiplication", PLDI 1994,
+// round-up variant): with l = ceil(log2 d) and m = floor(2^32 (2^l - d) / d) + 1,
+// n / d = (umulhi(n, m) + n) >> l for every 32-bit n (the sum taken in 64 bits).
+struct FastDiv {
+    uint32_t d, m, l;
+};
+inline FastDiv make_fastdiv(uint32_t d)
+{
+    FastDiv f{d, 0u, 0u};
+    if (d > 1) {
+        uint32_t l = 0;
+        while ((1ull << l) < d) ++l;
+        f.l = l;
+        f.m = static_cast<uint32_t>(((1ull << 32) * ((1ull << l) - d)) / d + 1);
+    }
+    return f;
+}
+#ifdef __CUDACC__
+__device__ __forceinline__ uint32_t fast_div(uint32_t n, const FastDiv& f)
+{
+    return static_cast<uint32_t>((static_cast<uint64_t>(__umulhi(n, f.m)) + n) >> f.l);
+}
+#endif
+
 // Device-side view handed to the kernel launchers.
 struct DomainDev {
     Geom g;
@@ -87,12 +134,14 @@ struct DomainDev {
     // handler writes (see the free-slip link note below).
     const int4* fs_link;
     int n_fs;
-    // Per interior fluid cell: which pull neighbours are not fluid (see classify_kernel).
-    uint32_t* link;
+    // Per interior fluid cell: x = which pull neighbours are not fluid (see classify_kernel);
+    // y = the cell's LinkRecord row, or kNoRecord.
+    uint2* link;
     // kFluidEdge cells as layout indices in increasing order: updated by the edge blocks of the
     // step kernel; all other fluid cells by its row blocks.
     const int* edge;
     int n_edge;
+    const LinkRecord* ltab;  // rows named by link[i].y
     // Device error word: set to 1 by a kernel whose bounded wait gave up.
     int* err;
     // Step monitor accumulators (kMonBuckets x 4 doubles, zero between steps).

@@ -113,7 +113,7 @@ __device__ __forceinline__ size_t ref_idx(const Geom& g, int x, int y, int z)
                (static_cast<size_t>(y) + static_cast<size_t>(g.yl + 2) * static_cast<size_t>(z));
 }
 
-__device__ __forceinline__ bool is_fluid(uint8_t f) { return f <= kFluidEdge; }
+__device__ __forceinline__ bool is_fluid(uint8_t f) { return f <= kFluidWall; }
 
 // ------------------------------------------------------------------------------------------
 // FP64 arithmetic in the reference's operation order (collision.hpp:6-70, boundary.hpp).
@@ -262,11 +262,11 @@ __device__ __forceinline__ void moments_shifted(const float (&s)[L::Q], float& d
 // sym = drho - rho uu/(2 cs2) + rho cu^2/(2 cs4) and differ in the sign of asym = rho cu/cs2:
 //   s_eq,q - ... = w_q (sym +- asym),   s_q <- s_q + omega (w_q (sym +- asym) - s_q).
 template <class L>
-__device__ __forceinline__ void collide_shifted(float (&s)[L::Q], float omega, double (&m)[4])
+__device__ __forceinline__ void collide_shifted(float (&s)[L::Q], float omega, float (&m)[4])
 {
     float drho, jx, jy, jz;
     moments_shifted<L>(s, drho, jx, jy, jz);
-    m[0] = 1.0 + static_cast<double>(drho);
+    m[0] = drho;
     m[1] = jx;
     m[2] = jy;
     m[3] = jz;
@@ -335,11 +335,13 @@ template <class S>
 struct StepParams {
     S* pop;
     const uint8_t* flag;
-    const uint32_t* link;  // per fluid cell: bit q = the pull neighbour x - c_q is not fluid
+    const uint2* link;     // per fluid cell: x bit q = the pull neighbour x - c_q is not fluid;
+                           // y = LinkRecord row or kNoRecord
     const BcEntry* bc;
     const double* profile;
     const int* edge;       // layout indices of the kFluidEdge cells, increasing
     int n_edge;
+    const LinkRecord* ltab;
     int* err;              // set to 1 when a bounded wait gives up
     double* mon;           // kMonBuckets x 4 FP64 accumulators of the step's mass and momentum,
                            // or nullptr
@@ -350,9 +352,12 @@ struct StepParams {
     float omega;
 };
 
-// Collides f in place; m receives the mass and momentum of the populations it started from.
+// Collides f in place; m receives the mass and momentum of the populations it started from, in
+// the compute type (shifted storage: the mass minus 1, so that nothing here needs FP64, whose
+// rate on this GPU is a small fraction of FP32's; the monitor converts inside its own branch).
 template <class L, class S>
-__device__ __forceinline__ void collide_any(typename Store<S>::C (&f)[L::Q], const StepParams<S>& P, double (&m)[4])
+__device__ __forceinline__ void collide_any(typename Store<S>::C (&f)[L::Q], const StepParams<S>& P,
+                                            typename Store<S>::C (&m)[4])
 {
     if constexpr (Store<S>::kShifted)
         collide_shifted<L>(f, P.omega, m);
@@ -362,19 +367,23 @@ __device__ __forceinline__ void collide_any(typename Store<S>::C (&f)[L::Q], con
 
 // Stores a cell's pre-collision mass and momentum for the adjoint's recompute segments.
 template <class S>
-__device__ __forceinline__ void record_moments(typename Store<S>::C* rec, int i, const double (&m)[4])
+__device__ __forceinline__ void record_moments(typename Store<S>::C* rec, int i, const typename Store<S>::C (&m)[4])
 {
     using T = typename Store<S>::C;
-    rec[4 * static_cast<size_t>(i) + 0] = static_cast<T>(m[0]);
-    rec[4 * static_cast<size_t>(i) + 1] = static_cast<T>(m[1]);
-    rec[4 * static_cast<size_t>(i) + 2] = static_cast<T>(m[2]);
-    rec[4 * static_cast<size_t>(i) + 3] = static_cast<T>(m[3]);
+    rec[4 * static_cast<size_t>(i) + 0] = Store<S>::kShifted ? T(1) + m[0] : m[0];
+    rec[4 * static_cast<size_t>(i) + 1] = m[1];
+    rec[4 * static_cast<size_t>(i) + 2] = m[2];
+    rec[4 * static_cast<size_t>(i) + 3] = m[3];
 }
 
-// Adds the warp's totals of m to one accumulator bucket. Every lane of the warp must call it.
-__device__ __forceinline__ void monitor_add(double* mon, const double (&m)[4])
+// Adds the warp's totals of m (the moments collide_any returned; zeros for a thread without a
+// cell, counted = false) to one accumulator bucket. Every lane of the warp must call it.
+template <class S>
+__device__ __forceinline__ void monitor_add(double* mon, const typename Store<S>::C (&m)[4], bool counted)
 {
-    double v[4] = {m[0], m[1], m[2], m[3]};
+    double v[4] = {static_cast<double>(m[0]), static_cast<double>(m[1]), static_cast<double>(m[2]),
+                   static_cast<double>(m[3])};
+    if (Store<S>::kShifted && counted) v[0] += 1.0;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1)
 #pragma unroll
@@ -386,11 +395,12 @@ __device__ __forceinline__ void monitor_add(double* mon, const double (&m)[4])
     }
 }
 
-// Handler values of an edge cell: for every direction p toward a non-fluid neighbour (bit inv(p)
-// of `link`), the value that neighbour's handler writes for this cell, stored where this cell
-// pulls direction inv(p) next step. fs[k * stride] holds the cell's post-collision populations.
-// Ghost-fluid and free-slip neighbours are skipped: their side passes fill those slots.
-template <class L, class S>
+// Handler values of an edge cell: for every direction p toward a non-fluid neighbour m (bit
+// inv(p) of `link`), the value m's handler writes for this cell, stored where this cell pulls
+// direction inv(p) next step: after an odd step plane inv(p) at the cell, after an even step
+// plane p at m. fs[k * stride] holds the cell's post-collision populations. Ghost-fluid and
+// free-slip neighbours are skipped: their side passes fill those slots.
+template <class L, class S, bool ODD>
 __device__ __forceinline__ void store_handler_values(const StepParams<S>& P, int x, int y, int z, int i,
                                                      uint32_t link, const typename Store<S>::C* fs,
                                                      int stride)
@@ -429,21 +439,21 @@ __device__ __forceinline__ void store_handler_values(const StepParams<S>& P, int
             val = bc_value_shifted<L>(be, p, fs, stride, m0, m1, m2, m3, vcell);
         else
             val = bc_value_exact<L>(be, p, fs, stride, m0, vcell);
-        St::st(P.pop + static_cast<size_t>(b) * P.g.PS + i, val);
+        if (ODD)
+            St::st(P.pop + static_cast<size_t>(b) * P.g.PS + i, val);
+        else
+            St::st(P.pop + static_cast<size_t>(p) * P.g.PS + cidx(P.g, mx, my, mz), val);
     }
 }
 
-// Post-collision stores of an edge cell: toward a fluid neighbour the plain AA store; toward a
-// non-fluid neighbour the raw value into that neighbour's slot (read back by
-// lbm_get_populations and lbm_moments). Targets wrap on periodic axes.
+// Post-collision stores of an edge cell: the plain AA stores, wrapping on periodic axes.
 template <class L, class S, bool ODD>
 __device__ __forceinline__ void store_edge_populations(const StepParams<S>& P, int x, int y, int z, int i,
-                                                       uint32_t link, const typename Store<S>::C (&f)[L::Q])
+                                                       const typename Store<S>::C (&f)[L::Q])
 {
 #pragma unroll
     for (int p = 0; p < L::Q; ++p) {
-        const bool to_boundary = (link >> inv<L>(p)) & 1u;
-        if (ODD || to_boundary) {
+        if (ODD) {
             int mx, my, mz;
             nbr_xyz(P.g, x, y, z, L::c(p, 0), L::c(p, 1), L::c(p, 2), mx, my, mz);
             Store<S>::st(P.pop + static_cast<size_t>(p) * P.g.PS + cidx(P.g, mx, my, mz), f[p]);
@@ -494,10 +504,17 @@ constexpr size_t stage_bytes()
     const size_t m = rows > scratch ? rows : scratch;
     return (m + 127) / 128 * 128;
 }
+// Shared memory of a row block: the staged rows, then (shifted storage) one LinkRecord per thread
+// (48 bytes, 16-byte aligned: the destination of its cp.async copies).
+template <class S>
+constexpr size_t link_smem_bytes()
+{
+    return Store<S>::kShifted ? static_cast<size_t>(kLinkWords) * kRowCells * 4 : 0;
+}
 template <class L, class S>
 constexpr size_t row_smem_bytes()
 {
-    return kSegs * stage_bytes<L, S>();
+    return kSegs * stage_bytes<L, S>() + link_smem_bytes<S>();
 }
 
 template <class L, class S, bool ODD>
@@ -508,19 +525,19 @@ __device__ __forceinline__ void edge_block(const StepParams<S>& P, int blk, unsi
     constexpr int Q = L::Q;
     const int tx = static_cast<int>(threadIdx.x);
     const int j = blk * kRowCells + tx;
-    double m[4] = {0.0, 0.0, 0.0, 0.0};
+    T m[4] = {T(0), T(0), T(0), T(0)};
     if (j < P.n_edge) {
         const int i = P.edge[j];
         const int r = i - kXOff;
         const int x = r % P.g.XS;
         const int t = r / P.g.XS;
         const int y = t % P.g.YS, z = t / P.g.YS;
-        const uint32_t link = P.link[i];
+        const uint32_t link = P.link[i].x;
         S* __restrict__ pop = P.pop;
         T f[Q];
 #pragma unroll
         for (int q = 0; q < Q; ++q) {
-            if (!ODD || ((link >> q) & 1u)) {
+            if (!ODD) {
                 f[q] = St::ld(pop + static_cast<size_t>(q) * P.g.PS + i);
             } else {
                 int nx, ny, nz;
@@ -530,27 +547,100 @@ __device__ __forceinline__ void edge_block(const StepParams<S>& P, int blk, unsi
         }
         collide_any<L, S>(f, P, m);
         if (P.rec) record_moments<S>(P.rec, i, m);
-        store_edge_populations<L, S, ODD>(P, x, y, z, i, link, f);
+        store_edge_populations<L, S, ODD>(P, x, y, z, i, f);
         if (link & ((1u << Q) - 1u)) {
             T* fs = reinterpret_cast<T*>(smem_raw) + tx;
 #pragma unroll
             for (int q = 0; q < Q; ++q) fs[q * kRowCells] = f[q];
-            store_handler_values<L, S>(P, x, y, z, i, link, fs, kRowCells);
+            store_handler_values<L, S, ODD>(P, x, y, z, i, link, fs, kRowCells);
         }
     }
-    if (P.mon) monitor_add(P.mon, m);
+    if (P.mon) monitor_add<S>(P.mon, m, j < P.n_edge);
 }
 
-__device__ __forceinline__ void segment_origin(const Geom& g, int seg, int nseg_x, int& x0, int& y, int& z)
+__device__ __forceinline__ void segment_origin(const Geom& g, int seg, const FastDiv& dx, const FastDiv& dy, int& x0,
+                                               int& y, int& z)
 {
-    x0 = 1 + (seg % nseg_x) * kRowCells;
-    const int yz = seg / nseg_x;
-    y = 1 + yz % g.yl;
-    z = 1 + yz / g.yl;
+    const uint32_t yz = fast_div(static_cast<uint32_t>(seg), dx);
+    x0 = 1 + (seg - static_cast<int>(yz * dx.d)) * kRowCells;
+    const uint32_t zz = fast_div(yz, dy);
+    y = 1 + static_cast<int>(yz - zz * dy.d);
+    z = 1 + static_cast<int>(zz);
+}
+
+// Handler values of a kFluidWall cell, after its collision. For every link ip = inv(p) (x + c_p
+// is a handler cell m) the cell stores m's handler value B_ip where it pulls it next step: after
+// an odd step slot ip at x, after an even step plane p at m. B_ip: no-slip f*_p; moving wall
+// f*_p + c rho; inflow c; outflow / pressure feq_ip(r0, j/r0) + feq_p(r0, j/r0) - f*_p, in
+// shifted form 2 w_p (r0 - 1 + r0 (cu_p^2 / (2 cs4) - |u|^2 / (2 cs2))) - f*_p (the odd terms
+// cancel), from the cell's LinkRecord rec (shifted storage only). ps and gy are the plane stride
+// and XS, hidden from the optimiser so that this path's address arithmetic stays in it.
+template <class L, class S, bool ODD>
+__device__ __forceinline__ void link_values(const StepParams<S>& P, int i, typename Store<S>::C (&f)[L::Q],
+                                            const typename Store<S>::C (&m)[4], uint32_t wl,
+                                            const uint32_t* rec, size_t ps, int gy)
+{
+    using St = Store<S>;
+    using T = typename St::C;
+    constexpr int Q = L::Q;
+    S* own = P.pop + i;
+    uint32_t spec = 0, valm = 0, wallm = 0;
+    float r0 = 1.f, ux = 0.f, uy = 0.f, uz = 0.f, uu_c = 0.f, rho = 1.f;
+    if constexpr (St::kShifted) {
+        if (rec) {
+            spec = rec[0];
+            wallm = rec[1];
+            valm = wallm | rec[2];
+            r0 = __uint_as_float(rec[3]);
+            const float ir0 = __uint_as_float(rec[4]);
+            ux = m[1] * ir0;
+            uy = m[2] * ir0;
+            uz = m[3] * ir0;
+            uu_c = (ux * ux + uy * uy + uz * uz) * kC;
+            rho = 1.f + m[0];
+        }
+    }
+#pragma unroll
+    for (int p = 0; p < Q; ++p) {
+        const int ip = inv<L>(p);
+        if (!((wl >> ip) & 1u)) continue;
+        T v = f[p];
+        if constexpr (St::kShifted) {
+            if ((spec >> ip) & 1u) {
+                if ((valm >> ip) & 1u) {
+                    const int k = min(__popc(valm & ((1u << ip) - 1u)), kMaxRecordValues - 1);
+                    const float c = __uint_as_float(rec[5 + k]);
+                    v = ((wallm >> ip) & 1u) ? fmaf(c, rho, f[p]) : c;
+                } else {
+                    const float cu = L::c(p, 0) * ux + L::c(p, 1) * uy + L::c(p, 2) * uz;
+                    v = 2.f * static_cast<float>(L::w(p)) * ((r0 - 1.f) + r0 * fmaf(cu * cu, kB, -uu_c)) - f[p];
+                }
+            }
+        }
+        if (ODD) {
+            St::st(own + static_cast<size_t>(ip) * ps, v);
+        } else {
+            const int off = L::c(p, 0) + L::c(p, 1) * gy + L::c(p, 2) * gy * P.g.YS;
+            St::st(own + static_cast<size_t>(p) * ps + off, v);
+        }
+    }
+}
+
+// The value v, hidden from the optimiser: address arithmetic that uses it stays inside the
+// (rarely taken) branch it is written in instead of being hoisted into registers held by every
+// thread of the kernel.
+template <class V>
+__device__ __forceinline__ V opaque(V v)
+{
+    if constexpr (sizeof(V) == 8)
+        asm volatile("" : "+l"(v));
+    else
+        asm volatile("" : "+r"(v));
+    return v;
 }
 
 template <class L, class S, bool ODD>
-__device__ __forceinline__ void row_block(const StepParams<S>& P, int rb, int nseg, int nseg_x,
+__device__ __forceinline__ void row_block(const StepParams<S>& P, int rb, int nseg, const FastDiv& dx, const FastDiv& dy,
                                           unsigned char* smem_raw, uint64_t* bars)
 {
     using St = Store<S>;
@@ -576,7 +666,7 @@ __device__ __forceinline__ void row_block(const StepParams<S>& P, int rb, int ns
         const int lane = tx;
         for (int s = 0; s < nsegs; ++s) {
             int x0, y, z;
-            segment_origin(P.g, seg0 + s, nseg_x, x0, y, z);
+            segment_origin(P.g, seg0 + s, dx, dy, x0, y, z);
             if (lane == 0) mbar_arrive_expect_tx(&bars[s], Q * bytes);
             __syncwarp();
             if (lane < Q) {
@@ -596,17 +686,36 @@ __device__ __forceinline__ void row_block(const StepParams<S>& P, int rb, int ns
     const int sz = P.g.XS * P.g.YS;
     for (int s = 0; s < nsegs; ++s) {
         int x0, y, z;
-        segment_origin(P.g, seg0 + s, nseg_x, x0, y, z);
+        segment_origin(P.g, seg0 + s, dx, dy, x0, y, z);
         const int x = x0 + tx;
         const int i = cidx(P.g, x, y, z);
-        bool bulk = x <= P.g.xl && P.flag[i] == kFluidBulk;
+        // links of a kFluidWall cell (bit q: x - c_q is a no-slip, moving-wall, inflow, outflow
+        // or pressure cell), and its LinkRecord, copied into shared memory while the rows are in
+        // flight (shifted storage). Cells on a face of the domain, where boundaries usually sit,
+        // load their link word together with their flag instead of after it.
+        const bool face = x == 1 || x == P.g.xl || y == 1 || y == P.g.yl || z == 1 || z == P.g.zl;
+        const uint2 lkf = face && x <= P.g.xl ? P.link[i] : make_uint2(0u, kNoRecord);
+        const uint8_t fl = x <= P.g.xl ? P.flag[i] : static_cast<uint8_t>(kFluidEdge);
+        bool bulk = fl == kFluidBulk || fl == kFluidWall;
+        const uint2 lk = fl != kFluidWall ? make_uint2(0u, kNoRecord) : face ? lkf : P.link[i];
+        const uint32_t wl = lk.x;
+        uint32_t* rec = nullptr;
+        if constexpr (St::kShifted) {
+            if (lk.y != kNoRecord) {
+                rec = reinterpret_cast<uint32_t*>(smem_raw + kSegs * SB) + kLinkWords * tx;
+                const char* src = reinterpret_cast<const char*>(P.ltab + lk.y);
+#pragma unroll
+                for (int w = 0; w < kLinkWords / 4; ++w) cp_async16(rec + 4 * w, src + 16 * w);
+                cp_async_commit();
+            }
+        }
         if (!mbar_wait_bounded(&bars[s], 0, kMaxPolls)) {
             // the step's results are invalid; still never leave while copies may land here
             *P.err = 1;
             mbar_wait_bounded(&bars[s], 0, kMaxPolls);
             bulk = false;
         }
-        double m[4] = {0.0, 0.0, 0.0, 0.0};
+        T m[4] = {T(0), T(0), T(0), T(0)};
         if (bulk) {
             const S* buf = reinterpret_cast<const S*>(smem_raw + s * SB);
             T f[Q];
@@ -614,6 +723,12 @@ __device__ __forceinline__ void row_block(const StepParams<S>& P, int rb, int ns
             for (int q = 0; q < Q; ++q) f[q] = St::ld(buf + q * W + PAD + tx - (ODD ? L::c(q, 0) : 0));
             collide_any<L, S>(f, P, m);
             if (P.rec) record_moments<S>(P.rec, i, m);
+            if (wl) {
+                if constexpr (St::kShifted) {
+                    if (rec) cp_async_wait_all();
+                }
+                link_values<L, S, ODD>(P, i, f, m, wl, rec, opaque(PS), opaque(sy));
+            }
 #pragma unroll
             for (int p = 0; p < Q; ++p) {
                 if (ODD) {
@@ -623,28 +738,57 @@ __device__ __forceinline__ void row_block(const StepParams<S>& P, int rb, int ns
                     St::st(pop + static_cast<size_t>(inv<L>(p)) * PS + i, f[p]);
                 }
             }
+        } else if constexpr (St::kShifted) {
+            if (rec) cp_async_wait_all();  // no copy may still be landing when the block ends
         }
-        if (P.mon) monitor_add(P.mon, m);
+        if (P.mon) monitor_add<S>(P.mon, m, bulk);
+    }
+}
+
+// Resident blocks per SM that the register allocation of a step kernel must allow (0: no
+// bound; ptxas then picks fewer registers than with an explicit 1). Unbounded, the shifted
+// D3Q19 kernels take 56 registers (9 blocks per SM); bounded to 10 blocks they keep 48. FP64 is
+// never bounded. LBMG_MINB_EVEN / LBMG_MINB_ODD override the shifted-storage
+// values in tuning builds.
+template <class L, class S, bool ODD>
+constexpr int min_blocks()
+{
+    if constexpr (!Store<S>::kShifted) {
+        return 0;
+    } else {
+#if defined(LBMG_MINB_ODD)
+        if (ODD) return LBMG_MINB_ODD;
+#endif
+#if defined(LBMG_MINB_EVEN)
+        if (!ODD) return LBMG_MINB_EVEN;
+#endif
+        return L::Q == 19 ? 10 : 0;
     }
 }
 
 // Edge blocks sit at every `edge_stride`-th block index (the first n_edge_blocks such
-// positions), so that the latency-bound edge work is spread over the whole launch instead of
-// holding the SMs at its start; the row blocks fill the other indices in order.
+// positions), so that the latency-bound edge work is spread over the first part of the launch
+// instead of holding the SMs at its start or running on after the last row block; the row
+// blocks fill the other indices in order.
+#ifndef LBMG_EDGE_SPAN
+#define LBMG_EDGE_SPAN 0.6
+#endif
+constexpr double kEdgeSpan = LBMG_EDGE_SPAN;
 template <class L, class S, bool ODD>
-__global__ void __launch_bounds__(kRowCells)
-    step_kernel(const StepParams<S> P, int n_edge_blocks, int edge_stride, int nseg, int nseg_x)
+__global__ void __launch_bounds__(kRowCells, min_blocks<L, S, ODD>())
+    step_kernel(const StepParams<S> P, int n_edge_blocks, FastDiv edge_stride, int nseg, FastDiv nseg_x, FastDiv yl)
 {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ __align__(8) uint64_t bars[kSegs];
     const int b = static_cast<int>(blockIdx.x);
-    const int interleaved = n_edge_blocks * edge_stride;
-    if (b < interleaved && b % edge_stride == 0)
-        edge_block<L, S, ODD>(P, b / edge_stride, smem_raw);
+    const int interleaved = n_edge_blocks * static_cast<int>(edge_stride.d);
+    const int e = static_cast<int>(fast_div(static_cast<uint32_t>(b), edge_stride));
+    if (b < interleaved && b == e * static_cast<int>(edge_stride.d))
+        edge_block<L, S, ODD>(P, e, smem_raw);
     else if (b < interleaved)
-        row_block<L, S, ODD>(P, b - (b / edge_stride + 1), nseg, nseg_x, smem_raw, bars);
+        row_block<L, S, ODD>(P, b - (e + 1), nseg, nseg_x, yl, smem_raw, bars);
     else
-        row_block<L, S, ODD>(P, b - n_edge_blocks, nseg, nseg_x, smem_raw, bars);
+        row_block<L, S, ODD>(P, b - n_edge_blocks, nseg, nseg_x, yl, smem_raw, bars);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -658,11 +802,10 @@ __device__ __forceinline__ typename Store<S>::C load_post(const S* pop, const ui
                                                           const Geom& g, int x, int y, int z,
                                                           int i, int p, bool odd)
 {
+    if (!odd) return Store<S>::ld(pop + static_cast<size_t>(inv<L>(p)) * g.PS + i);
     int mx, my, mz;
     nbr_xyz(g, x, y, z, L::c(p, 0), L::c(p, 1), L::c(p, 2), mx, my, mz);
-    const int m = cidx(g, mx, my, mz);
-    if (!odd && is_fluid(flag[m])) return Store<S>::ld(pop + static_cast<size_t>(inv<L>(p)) * g.PS + i);
-    return Store<S>::ld(pop + static_cast<size_t>(p) * g.PS + m);
+    return Store<S>::ld(pop + static_cast<size_t>(p) * g.PS + cidx(g, mx, my, mz));
 }
 
 // collide_field populations of any cell as FP64 (see lbm_get_populations). Ghost-fluid cells
@@ -687,7 +830,9 @@ __device__ __forceinline__ void load_cell_f64(const S* pop, const uint8_t* flag,
         if (fl >= kFirstHandler && interior(g, nx, ny, nz)) {
             const int n = cidx(g, nx, ny, nz);
             if (is_fluid(flag[n]))
-                v = to_f64<L, S>(Store<S>::ld(pop + static_cast<size_t>(q) * g.PS + n), q);
+                v = to_f64<L, S>(odd ? Store<S>::ld(pop + static_cast<size_t>(q) * g.PS + n)
+                                     : Store<S>::ld(pop + static_cast<size_t>(inv<L>(q)) * g.PS + i),
+                                 q);
         }
         out[q] = v;
     }

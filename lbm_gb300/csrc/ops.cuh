@@ -34,6 +34,8 @@ struct KernelOps {
     // mu_t -> mu_{t-1} with the record of step t-1; theta gradients of step t
     void (*adj_step)(const DomainDev& d, const void* mu_in, void* mu_out, const void* rec, int bc_terms,
                      int write_mu, double* grad_inflow, double* grad_wall, cudaStream_t s);
+    // LinkRecords of the kFluidWall cells with non-no-slip links (capacity 0: count only)
+    void (*link_table)(const DomainDev& d, LinkRecord* ltab, int* counter, int capacity, cudaStream_t s);
     // kinetic energy of the box into out[0] (device), partials as for reduce
     void (*objective_ke)(const DomainDev& d, long long k, Box box, double* partials, int reduce_blocks,
                          double* out, cudaStream_t s);

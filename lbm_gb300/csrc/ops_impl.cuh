@@ -2,6 +2,8 @@
 // and step_bf16.cu, each of which defines LBMG_STORE and LBMG_OPS_NAME before including it.
 #pragma once
 
+#include <algorithm>
+
 #include "ops.cuh"
 #include "state_kernels.cuh"
 #include "adjoint.cuh"
@@ -31,6 +33,7 @@ StepParams<S> step_params(const DomainDev& d)
     p.bc = d.bc;
     p.edge = d.edge;
     p.n_edge = d.n_edge;
+    p.ltab = d.ltab;
     p.profile = d.profile;
     p.g = d.g;
     p.err = d.err;
@@ -52,7 +55,7 @@ struct Launch {
 
     static void classify(const DomainDev& d, cudaStream_t s)
     {
-        classify_kernel<L><<<cell_grid(d.g), kBlockX, 0, s>>>(d.flag, d.link, d.g);
+        classify_kernel<L><<<cell_grid(d.g), kBlockX, 0, s>>>(d.flag, d.link, d.bc, d.g, Store<S>::kShifted);
     }
 
     static void side_passes(const DomainDev& d, long long k, cudaStream_t s)
@@ -77,8 +80,15 @@ struct Launch {
         const int row_blocks = (nseg + kSegs - 1) / kSegs;
         const int n_edge_blocks = (d.n_edge + kRowCells - 1) / kRowCells;
         const long long total = static_cast<long long>(n_edge_blocks) + row_blocks;
-        const int edge_stride = n_edge_blocks > 0 ? static_cast<int>(total / n_edge_blocks) : 1;
+        // An edge block runs several times longer than a row block (gathers, handler lookups):
+        // spread over the whole grid, the last ones would still run after every row block has
+        // finished. They are spread over the first kEdgeSpan of the grid instead.
+        const long long span = std::max<long long>(n_edge_blocks, static_cast<long long>(total * kEdgeSpan));
+        const int edge_stride = n_edge_blocks > 0 ? static_cast<int>(std::max<long long>(1, span / n_edge_blocks)) : 1;
         const unsigned blocks = static_cast<unsigned>(total);
+        const FastDiv fes = make_fastdiv(static_cast<uint32_t>(edge_stride));
+        const FastDiv fx = make_fastdiv(static_cast<uint32_t>(nseg_x));
+        const FastDiv fy = make_fastdiv(static_cast<uint32_t>(d.g.yl));
         constexpr size_t smem = row_smem_bytes<L, S>();
         if constexpr (smem > 48 * 1024) {
             static bool opted_in = false;
@@ -91,9 +101,9 @@ struct Launch {
             }
         }
         if (t & 1)
-            step_kernel<L, S, true><<<blocks, kRowCells, smem, s>>>(p, n_edge_blocks, edge_stride, nseg, nseg_x);
+            step_kernel<L, S, true><<<blocks, kRowCells, smem, s>>>(p, n_edge_blocks, fes, nseg, fx, fy);
         else
-            step_kernel<L, S, false><<<blocks, kRowCells, smem, s>>>(p, n_edge_blocks, edge_stride, nseg, nseg_x);
+            step_kernel<L, S, false><<<blocks, kRowCells, smem, s>>>(p, n_edge_blocks, fes, nseg, fx, fy);
         if (mon_out) monitor_final_kernel<<<1, 256, 0, s>>>(d.mon, mon_out);
         side_passes(d, t, s);
     }
@@ -172,10 +182,17 @@ struct Launch {
         reduce_final_kernel<<<1, 32, 0, s>>>(partials, nblocks, out);
     }
 
+    static void link_table(const DomainDev& d, LinkRecord* ltab, int* counter, int capacity, cudaStream_t s)
+    {
+        link_table_kernel<L><<<cell_grid(d.g), kBlockX, 0, s>>>(d.flag, d.link, d.bc, d.profile, d.g, ltab, counter,
+                                                                 capacity);
+    }
+
     static const KernelOps* table()
     {
-        static const KernelOps t = {&init,    &classify, &step,      &gather,       &scatter,  &moments,
-                                    &reduce,  sizeof(T), &adj_terminal, &adj_step, &objective_ke};
+        static const KernelOps t = {&init,     &classify, &step,         &gather,   &scatter,
+                                    &moments,  &reduce,   sizeof(T),     &adj_terminal, &adj_step,
+                                    &link_table, &objective_ke};
         return &t;
     }
 };

@@ -24,30 +24,95 @@ __global__ void init_kernel(S* pop, size_t PS)
 // wrap, else kFluidBulk; and their link word (bit q: the pull neighbour x - c_q is not fluid).
 // The lattice is symmetric, so the pull neighbours x - c_q are also all the push neighbours.
 template <class L>
-__global__ void classify_kernel(uint8_t* flag, uint32_t* link, Geom g)
+// special_ok (shifted storage): links to moving-wall, inflow, outflow and pressure cells (at most
+// at most kMaxRecordValues moving-wall and inflow links, one outlet density) keep a cell in the
+// row blocks, served by its LinkRecord.
+__global__ void classify_kernel(uint8_t* flag, uint2* link, const BcEntry* bc, Geom g, bool special_ok)
 {
     const int x = 1 + static_cast<int>(blockIdx.x) * kBlockX + static_cast<int>(threadIdx.x);
     if (x > g.xl) return;
     const int y = 1 + static_cast<int>(blockIdx.y), z = 1 + static_cast<int>(blockIdx.z);
     const int i = cidx(g, x, y, z);
     if (!is_fluid(flag[i])) return;
-    bool edge = false;
+    bool edge = false;  // some neighbour wraps or needs the edge path's handling
     uint32_t m = 0;
+    int values = 0;      // moving-wall and inflow links (one LinkRecord value each)
+    double r0 = -1.0;    // reference density of the outflow / pressure links
 #pragma unroll
     for (int q = 0; q < L::Q; ++q) {
         const int ax = x - L::c(q, 0), ay = y - L::c(q, 1), az = z - L::c(q, 2);
         int nx, ny, nz;
         nbr_xyz(g, x, y, z, -L::c(q, 0), -L::c(q, 1), -L::c(q, 2), nx, ny, nz);
         if (nx != ax || ny != ay || nz != az) edge = true;
-        // flags of fluid cells only move between kFluidBulk and kFluidEdge here, so this read
-        // of a neighbour's flag sees the same fluid / non-fluid answer whatever the timing
-        if (!is_fluid(flag[cidx(g, nx, ny, nz)])) {
-            edge = true;
+        // flags of fluid cells only move among the fluid values here, so this read of a
+        // neighbour's flag sees the same fluid / non-fluid answer whatever the timing
+        const uint8_t fn = flag[cidx(g, nx, ny, nz)];
+        if (!is_fluid(fn)) {
             m |= 1u << q;
+            const int t = fn < kFirstHandler ? -1 : bc[fn - kFirstHandler].type;
+            if (t == kNoSlip) {
+            } else if (special_ok && (t == kMovingWall || t == kInflow)) {
+                ++values;
+            } else if (special_ok && (t == kOutflow || t == kPressure)) {
+                const double r = bc[fn - kFirstHandler].rho;
+                if (r0 >= 0.0 && r != r0) edge = true;  // one outlet density per cell
+                r0 = r;
+            } else {
+                edge = true;
+            }
         }
     }
-    flag[i] = edge ? kFluidEdge : kFluidBulk;
-    link[i] = m;
+    if (values > kMaxRecordValues) edge = true;
+    flag[i] = edge ? kFluidEdge : (m ? kFluidWall : kFluidBulk);
+    link[i] = make_uint2(m, kNoRecord);
+}
+
+// LinkRecord of every kFluidWall cell with links to handlers other than no-slip (shifted
+// storage). Rows are handed out by an atomic counter; with capacity 0 it only counts them.
+template <class L>
+__global__ void link_table_kernel(const uint8_t* flag, uint2* link, const BcEntry* bc, const double* profile,
+                                  Geom g, LinkRecord* ltab, int* counter, int capacity)
+{
+    const int x = 1 + static_cast<int>(blockIdx.x) * kBlockX + static_cast<int>(threadIdx.x);
+    if (x > g.xl) return;
+    const int y = 1 + static_cast<int>(blockIdx.y), z = 1 + static_cast<int>(blockIdx.z);
+    const int i = cidx(g, x, y, z);
+    if (flag[i] != kFluidWall) return;
+    const uint32_t lk = link[i].x;
+    LinkRecord r{};
+    int k = 0;
+    for (int q = 0; q < L::Q; ++q) {
+        if (!((lk >> q) & 1u)) continue;
+        int nx, ny, nz;
+        nbr_xyz(g, x, y, z, -rt_c<L>(q, 0), -rt_c<L>(q, 1), -rt_c<L>(q, 2), nx, ny, nz);
+        const BcEntry& be = bc[flag[cidx(g, nx, ny, nz)] - kFirstHandler];
+        if (be.type == kNoSlip) continue;
+        r.spec |= 1u << q;
+        if (be.type == kOutflow || be.type == kPressure) {
+            r.r0 = static_cast<float>(be.rho);
+            r.ir0 = 1.f / r.r0;
+            continue;
+        }
+        if (k >= kMaxRecordValues) continue;  // classify sent such cells to the edge blocks
+        if (be.type == kMovingWall) {
+            const float cu = rt_c<L>(q, 0) * static_cast<float>(be.v[0]) + rt_c<L>(q, 1) * static_cast<float>(be.v[1]) +
+                             rt_c<L>(q, 2) * static_cast<float>(be.v[2]);
+            r.wall |= 1u << q;
+            r.c[k++] = 2.f * static_cast<float>(rt_w<L>(q)) * cu * kA;
+        } else {
+            const double* v = be.has_profile ? profile + 3 * ref_idx(g, nx, ny, nz) : be.v;
+            const float rr = static_cast<float>(be.rho);
+            const float ux = static_cast<float>(v[0]), uy = static_cast<float>(v[1]), uz = static_cast<float>(v[2]);
+            r.inflow |= 1u << q;
+            r.c[k++] = seq_shifted<L>(q, rr - 1.f, rr, ux, uy, uz, (ux * ux + uy * uy + uz * uz) * kC);
+        }
+    }
+    if (!r.spec) return;
+    const int row = atomicAdd(counter, 1);
+    if (row < capacity) {
+        link[i].y = static_cast<uint32_t>(row);
+        ltab[row] = r;
+    }
 }
 
 // Device layout -> AoS FP64 field over all cells (reference cell order).
@@ -80,14 +145,14 @@ __global__ void scatter_kernel(S* pop, const uint8_t* flag, Geom g, int odd, con
     const size_t r = ref_idx(g, x, y, z);
 #pragma unroll
     for (int p = 0; p < L::Q; ++p) {
-        int mx, my, mz;
-        nbr_xyz(g, x, y, z, L::c(p, 0), L::c(p, 1), L::c(p, 2), mx, my, mz);
-        const int m = cidx(g, mx, my, mz);
         const auto v = from_f64<L, S>(in[r * L::Q + p], p);
-        if (!odd && is_fluid(flag[m]))
+        if (!odd) {
             Store<S>::st(pop + static_cast<size_t>(inv<L>(p)) * g.PS + i, v);
-        else
-            Store<S>::st(pop + static_cast<size_t>(p) * g.PS + m, v);
+        } else {
+            int mx, my, mz;
+            nbr_xyz(g, x, y, z, L::c(p, 0), L::c(p, 1), L::c(p, 2), mx, my, mz);
+            Store<S>::st(pop + static_cast<size_t>(p) * g.PS + cidx(g, mx, my, mz), v);
+        }
     }
 #pragma unroll
     for (int q = 0; q < L::Q; ++q) {
@@ -96,7 +161,10 @@ __global__ void scatter_kernel(S* pop, const uint8_t* flag, Geom g, int odd, con
         const int n = cidx(g, nx, ny, nz);
         if (is_fluid(flag[n])) continue;
         const auto v = from_f64<L, S>(in[ref_idx(g, nx, ny, nz) * L::Q + q], q);
-        Store<S>::st(pop + static_cast<size_t>(q) * g.PS + i, v);
+        if (odd)
+            Store<S>::st(pop + static_cast<size_t>(q) * g.PS + i, v);
+        else
+            Store<S>::st(pop + static_cast<size_t>(inv<L>(q)) * g.PS + n, v);
     }
 }
 
@@ -195,6 +263,19 @@ static __global__ void reduce_final_kernel(const double* partials, int nblocks, 
 // is collided at step t. Interior fluid cells pull from them. Copy (t mod 2) is collided after
 // step t and written into the boundary slots of the neighbours, which pull it at step t + 1.
 // ------------------------------------------------------------------------------------------
+// Stores the value that non-fluid cell b = (bx, by, bz) hands to its fluid neighbour n = b + c_q
+// (layout index n), where n pulls it next step: after an odd step plane q at n, after an even
+// step plane inv(q) at b.
+template <class L, class S>
+__device__ __forceinline__ void store_slot(S* pop, const Geom& g, int odd, int n, int bx, int by, int bz, int q,
+                                           typename Store<S>::C v)
+{
+    if (odd)
+        Store<S>::st(pop + static_cast<size_t>(q) * g.PS + n, v);
+    else
+        Store<S>::st(pop + static_cast<size_t>(L::Q - 1 - q) * g.PS + cidx(g, bx, by, bz), v);
+}
+
 template <class L, class S>
 __global__ void ghost_fluid_kernel(S* pop, const uint8_t* flag, Geom g, double tau,
                                    const int* gf_xyz, double* gf_pop, int n_gf, int copy)
@@ -215,8 +296,7 @@ __global__ void ghost_fluid_kernel(S* pop, const uint8_t* flag, Geom g, double t
         nbr_xyz(g, x, y, z, L::c(q, 0), L::c(q, 1), L::c(q, 2), nx, ny, nz);
         if (!interior(g, nx, ny, nz)) continue;
         const int n = cidx(g, nx, ny, nz);
-        if (is_fluid(flag[n]))
-            Store<S>::st(pop + static_cast<size_t>(q) * g.PS + n, from_f64<L, S>(f[q], q));
+        if (is_fluid(flag[n])) store_slot<L, S>(pop, g, copy, n, x, y, z, q, from_f64<L, S>(f[q], q));
     }
 }
 
@@ -249,8 +329,7 @@ __global__ void ghost_fluid_slots_kernel(S* pop, const uint8_t* flag, Geom g, co
         nbr_xyz(g, x, y, z, L::c(q, 0), L::c(q, 1), L::c(q, 2), nx, ny, nz);
         if (!interior(g, nx, ny, nz)) continue;
         const int n = cidx(g, nx, ny, nz);
-        if (is_fluid(flag[n]))
-            Store<S>::st(pop + static_cast<size_t>(q) * g.PS + n, from_f64<L, S>(c[q], q));
+        if (is_fluid(flag[n])) store_slot<L, S>(pop, g, copy, n, x, y, z, q, from_f64<L, S>(c[q], q));
     }
 }
 
@@ -273,12 +352,16 @@ __global__ void free_slip_kernel(S* pop, const uint8_t* flag, Geom g, const int4
     typename Store<S>::C v;
     if (kind == 1) {
         v = from_f64<L, S>(gf_pop[(static_cast<size_t>(copy) * n_gf + l.z) * L::Q + qs], qs);
-    } else if (!odd && is_fluid(flag[l.w])) {
+    } else if (!odd) {
         v = Store<S>::ld(pop + static_cast<size_t>(L::Q - 1 - qs) * g.PS + l.z);
     } else {
         v = Store<S>::ld(pop + static_cast<size_t>(qs) * g.PS + l.w);
     }
-    Store<S>::st(pop + static_cast<size_t>(q) * g.PS + l.x, v);
+    // the free-slip cell b = dst - c_q
+    const int r = l.x - kXOff;
+    int bx, by, bz;
+    nbr_xyz(g, r % g.XS, (r / g.XS) % g.YS, r / (g.XS * g.YS), -rt_c<L>(q, 0), -rt_c<L>(q, 1), -rt_c<L>(q, 2), bx, by, bz);
+    store_slot<L, S>(pop, g, odd, l.x, bx, by, bz, q, v);
 }
 
 }  // namespace lbmg

@@ -47,26 +47,40 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
         : "memory");
 }
 
+// One poll of phase `parity` of `bar`. The thread may sleep up to kWaitHintNs inside it while the
+// phase is incomplete (it wakes as soon as the phase completes), so that a waiting warp issues a
+// handful of polls instead of spinning.
+constexpr uint32_t kWaitHintNs = 2000;
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
 {
     uint32_t ok;
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
         "selp.u32 %0, 1, 0, p;\n\t}"
         : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(parity)
+        : "r"(smem_u32(bar)), "r"(parity), "r"(kWaitHintNs)
         : "memory");
     return ok != 0;
 }
 
-// Waits for phase `parity` of `bar` with a bounded number of polls. Returns false (and the
-// caller reports an error) if the phase did not complete in time.
+// Waits for phase `parity` of `bar` with a bounded number of polls (at most about
+// max_polls * kWaitHintNs). Returns false (and the caller reports an error) if the phase did not
+// complete in time.
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, uint32_t max_polls)
 {
     for (uint32_t k = 0; k < max_polls; ++k)
         if (mbar_try_wait(bar, parity)) return true;
     return false;
 }
+
+// Asynchronous 16-byte copy global -> shared (both 16-byte aligned), and the wait for all of the
+// calling thread's such copies.
+__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gmem_src)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(smem_dst)), "l"(gmem_src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
 }  // namespace lbmg
