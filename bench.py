@@ -41,6 +41,8 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--size", default="256,128,128")
     ap.add_argument("--quick", action="store_true", help="headline only (no stencil sweep / e2e / cpu)")
+    ap.add_argument("--extra-only", action="store_true",
+                    help="only the Taylor-Green, 512^3 cavity and cavity-adjoint workloads")
     return ap.parse_args()
 
 
@@ -249,6 +251,9 @@ def run_ours(args, rank, world, local):
     line.update(out_extra)
     if not args.quick:
         line["adjoint"] = run_adjoint()
+        line["taylor_green"] = run_taylor_green()
+        line["cavity512_d3q27"] = run_large_cavity()
+        line["cavity256_adjoint"] = run_cavity_adjoint()
         line["e2e"] = run_e2e(scn19, K, W)
         if rank == 0:
             line["cpu_baseline"] = cpu_baseline(size, budget_s=12.0)
@@ -323,6 +328,125 @@ def run_adjoint(xl=128, yl=64, zl=64, steps=2000, ckpt=100):
         "timing": "wall clock around synchronised calls (backward includes its allocations and the "
                   "gradient download); plain steps by CUDA events",
     }
+
+
+def _rel_l2(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def run_taylor_green(n=384, u0=0.03, omega=1.9, steps=2000):
+    """Decaying Taylor-Green vortex, D3Q19 periodic n^3, f = feq(1, u_TG) at start: FP32 / BF16 /
+    FP16 shifted storage against the FP64 GPU run of the same steps (relative L2 of u and of
+    rho - 1), and the kinetic energy against the linear decay E0 exp(-6 nu k^2 t),
+    nu = cs^2 (tau - 1/2), k = 2 pi / n (a low-Reynolds guide: Re = u0 / (nu k) here)."""
+    from lbm_gb300 import build_domain
+    from lbm_gb300 import scenario as S
+    scn = S.taylor_green(n, u0, omega)
+    out = {"workload": f"Taylor-Green D3Q19 {n}^3 periodic, u0 {u0}, omega {omega}, {steps} steps", "steps": steps}
+    ref = None
+    nu = (1.0 / omega - 0.5) / 3.0
+    k = 2 * np.pi / n
+    u_init = S.taylor_green_velocity(n, u0)
+    ke0 = 0.5 * float((u_init ** 2).sum())
+    del u_init
+    for prec in ("fp64", "fp32", "bf16", "fp16"):
+        with build_domain(scn, prec) as d:
+            sec = time_steps(d, steps, 0)
+            rho, u = d.moments()
+        ke = 0.5 * float((rho * (u ** 2).sum(axis=-1)).sum())
+        r = {"mlups": n ** 3 * steps / sec / 1e6, "ke_over_ke0": ke / ke0}
+        if ref is None:
+            ref = (rho, u)
+            r["ke_linear_decay_ratio"] = ke / (ke0 * np.exp(-6 * nu * k * k * steps))
+        else:
+            r["u_rel_l2_vs_fp64"] = _rel_l2(u, ref[1])
+            r["rho_rel_l2_vs_fp64"] = _rel_l2(rho - 1.0, ref[0] - 1.0)
+        out[prec] = r
+        del rho, u
+    out["reynolds"] = u0 / (nu * k)
+    return out
+
+
+def run_large_cavity(n=512, q=27, omega=1.95, lid=0.1, steps=500, n_acc=128, omega_acc=1.8):
+    """D3Q27 lid-driven cavity n^3 with FP16 shifted storage (AA in place) and, beside it, FP32:
+    `steps` steps timed. At omega 1.95 (tau 0.513) and lid 0.1 the BGK cavity diverges within
+    these steps in every precision, FP64 included (the reference's scheme, reproduced bit for bit
+    in FP64, behaves the same), so the velocity errors are stated on an n_acc^3 cavity at
+    omega_acc, where the same 500 steps stay stable: FP16 / BF16 / FP32 against FP64."""
+    from lbm_gb300 import build_domain
+    from lbm_gb300 import scenario as S
+    peak, _ = measured_peak()
+    out = {"workload": f"cavity D3Q{q} {n}^3, lid {lid}, omega {omega}, {steps} steps", "cells": n ** 3}
+    for prec in ("fp16", "fp32"):
+        with build_domain(S.cavity(n, q=q, lid=lid, tau=1.0 / omega), prec) as d:
+            info = d.memory_info()
+            sec = time_steps(d, steps, 0)
+            rho, _ = d.moments()
+        fin = np.isfinite(rho)
+        out[prec] = {"mlups": n ** 3 * steps / sec / 1e6, "ms_per_step": sec / steps * 1e3,
+                     "hbm_frac": info["step_bytes"] / (sec / steps) / 1e9 / peak,
+                     "device_bytes": info["device_bytes"],
+                     "final_rho_range": [float(rho[fin].min()), float(rho[fin].max())] if fin.any() else None,
+                     "non_finite_cells": int((~fin).sum())}
+        del rho
+    acc = {"workload": f"cavity D3Q{q} {n_acc}^3, lid {lid}, omega {omega_acc}, {steps} steps"}
+    us = {}
+    for prec in ("fp64", "fp32", "fp16", "bf16"):
+        with build_domain(S.cavity(n_acc, q=q, lid=lid, tau=1.0 / omega_acc), prec) as d:
+            d.step(steps)
+            rho, us[prec] = d.moments()
+        if prec == "fp64":
+            acc["fp64_rho_range"] = [float(rho.min()), float(rho.max())]
+    for prec in ("fp32", "fp16", "bf16"):
+        acc[f"u_rel_l2_{prec}_vs_fp64"] = _rel_l2(us[prec], us["fp64"])
+    out["accuracy"] = acc
+    return out
+
+
+def run_cavity_adjoint(n=256, q=27, omega=1.8, lid=0.1, steps=500, ckpt=50, n_fd=128):
+    """Gradient of the cavity's kinetic energy after `steps` steps with respect to the lid
+    velocity, FP16 storage (FP32 adjoint arithmetic), checkpoints every `ckpt` steps, timed
+    against plain FP16 steps on n^3. omega 1.8: at 1.95 the forward run itself diverges. dJ/du_x is
+    checked on an n_fd^3 cavity against FP64 central differences (h = 1e-6)."""
+    import torch
+    from lbm_gb300 import build_domain
+    from lbm_gb300 import scenario as S
+
+    def make(m, v):
+        return S.cavity(m, q=q, lid=v, tau=1.0 / omega)
+    box = (1, n, 1, n, 1, n)
+    with build_domain(make(n, lid), "fp16") as d:
+        plain = time_steps(d, steps, 0)
+    with build_domain(make(n, lid), "fp16") as d:
+        d.step(0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        d.adjoint_forward(steps, ckpt)
+        d.sync()
+        t1 = time.perf_counter()
+        _, gw = d.adjoint_backward(box)
+        t2 = time.perf_counter()
+    fbox = (1, n_fd, 1, n_fd, 1, n_fd)
+    with build_domain(make(n_fd, lid), "fp16") as d:
+        d.adjoint_forward(steps, ckpt)
+        _, gw_fd = d.adjoint_backward(fbox)
+    h = 1e-6
+    vals = []
+    for sgn in (1, -1):
+        with build_domain(make(n_fd, lid + sgn * h), "fp64") as d:
+            d.step(steps)
+            vals.append(d.objective_ke(fbox))
+    fd = (vals[0] - vals[1]) / (2 * h)
+    return {"workload": f"cavity D3Q{q} {n}^3 adjoint wrt lid velocity, lid {lid}, omega {omega}, {steps} steps, "
+                        f"checkpoint every {ckpt}, J = KE of the whole cavity",
+            "storage": "fp16 (f - w), adjoint in fp32",
+            "forward_plain_ms_per_step": plain / steps * 1e3,
+            "forward_ckpt_ms_per_step": (t1 - t0) / steps * 1e3,
+            "backward_ms_per_step": (t2 - t1) / steps * 1e3,
+            "backward_over_forward": (t2 - t1) / plain,
+            "dJ_du_lid": [float(x) for x in gw[1]],
+            "fd_check": {"cells": n_fd ** 3, "fd_fp64_dJ_du_x": fd, "adjoint_fp16_dJ_du_x": float(gw_fd[1][0]),
+                         "rel_err": abs(gw_fd[1][0] - fd) / abs(fd)}}
 
 
 def run_e2e(scn, K, W):
@@ -436,6 +560,13 @@ def main():
         line = run_reference(args, rank, world)
         if line is not None:
             print(json.dumps(line), flush=True)
+        return
+    if args.extra_only:
+        import torch
+        torch.cuda.set_device(local)
+        line = {"adjoint": run_adjoint(), "taylor_green": run_taylor_green(), "cavity512_d3q27": run_large_cavity(),
+                "cavity256_adjoint": run_cavity_adjoint()}
+        print(json.dumps(line), flush=True)
         return
     if world > 1:
         import torch.distributed as dist

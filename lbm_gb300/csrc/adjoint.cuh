@@ -25,6 +25,7 @@ template <class T>
 struct AdjParams {
     const uint8_t* flag;
     const uint2* link;
+    const LinkRecord* ltab;  // handler records of kFluidWall cells (shifted storage), or nullptr
     const BcEntry* bc;
     const double* profile;
     Geom g;
@@ -130,33 +131,52 @@ __global__ void __launch_bounds__(kBlockX) adjoint_step_kernel(const AdjParams<T
     if (active) {
         const size_t PS = A.g.PS;
         T lam[Q];
-        // transposed pull: x's f*_p became the pulled g_p of x + c_p
+        // transposed pull: x's f*_p became the pulled g_p of x + c_p. Non-fluid cells hold 0 in
+        // every adjoint array (cleared once, never written), so no neighbour test is needed; bulk
+        // cells have no wrapped neighbour either.
+        if (fl != kFluidEdge) {  // no wrapped neighbour
 #pragma unroll
-        for (int p = 0; p < Q; ++p) {
-            int mx, my, mz;
-            nbr_xyz(A.g, x, y, z, L::c(p, 0), L::c(p, 1), L::c(p, 2), mx, my, mz);
-            const int m = cidx(A.g, mx, my, mz);
-            lam[p] = is_fluid(A.flag[m]) ? A.mu_in[static_cast<size_t>(p) * PS + m] : T(0);
+            for (int p = 0; p < Q; ++p) {
+                const long long off = static_cast<long long>(p) * static_cast<long long>(PS) + L::c(p, 0) +
+                                      L::c(p, 1) * A.g.XS + static_cast<long long>(L::c(p, 2)) * A.g.XS * A.g.YS;
+                lam[p] = (A.mu_in + off)[i];
+            }
+        } else {
+#pragma unroll
+            for (int p = 0; p < Q; ++p) {
+                int mx, my, mz;
+                nbr_xyz(A.g, x, y, z, L::c(p, 0), L::c(p, 1), L::c(p, 2), mx, my, mz);
+                lam[p] = A.mu_in[static_cast<size_t>(p) * PS + cidx(A.g, mx, my, mz)];
+            }
         }
         const T rho_s = A.rec[4 * static_cast<size_t>(i) + 0];
         const T jxs = A.rec[4 * static_cast<size_t>(i) + 1];
         const T jys = A.rec[4 * static_cast<size_t>(i) + 2];
         const T jzs = A.rec[4 * static_cast<size_t>(i) + 3];
-        const uint32_t link = fl != kFluidBulk ? A.link[i].x : 0u;
+        const uint2 lw = fl != kFluidBulk ? A.link[i] : make_uint2(0u, kNoRecord);
+        const uint32_t link = lw.x;
+        // links whose handler needs its table entry: every link of a kFluidEdge cell; of a
+        // kFluidWall cell only those its LinkRecord lists (the others are no-slip)
+        uint32_t generic = link;
+        if (fl == kFluidWall) generic = (lw.y != kNoRecord && A.ltab) ? A.ltab[lw.y].spec : 0u;
         if (A.bc_terms && link) {
             T spread = 0;              // added to every direction (handlers that use sum f*)
             T sx = 0, sy = 0, sz = 0;  // outflow / pressure: added as c_p . s
 #pragma unroll
             for (int q = 0; q < Q; ++q) {
                 if (!((link >> q) & 1u)) continue;
+                const T mu_q = A.mu_in[static_cast<size_t>(q) * PS + i];
+                const int qb = L::Q - 1 - q;
+                if (!((generic >> q) & 1u)) {  // no-slip: B_q = f*_qb
+                    lam[qb] += mu_q;
+                    continue;
+                }
                 int bx, by, bz;
                 nbr_xyz(A.g, x, y, z, -L::c(q, 0), -L::c(q, 1), -L::c(q, 2), bx, by, bz);
                 const uint8_t flb = A.flag[cidx(A.g, bx, by, bz)];
                 if (flb < kFirstHandler) continue;
                 const int h = flb - kFirstHandler;
                 const BcEntry& be = A.bc[h];
-                const T mu_q = A.mu_in[static_cast<size_t>(q) * PS + i];
-                const int qb = L::Q - 1 - q;
                 switch (be.type) {
                 case kNoSlip:  // B_q = f*_qb
                     lam[qb] += mu_q;
@@ -218,7 +238,7 @@ __global__ void __launch_bounds__(kBlockX) adjoint_step_kernel(const AdjParams<T
         if (A.write_mu) {
             bgk_adjoint<L, T>(lam, rho_s, jxs, jys, jzs, A.omega);
 #pragma unroll
-            for (int p = 0; p < Q; ++p) A.mu_out[static_cast<size_t>(p) * PS + i] = lam[p];
+            for (int p = 0; p < Q; ++p) (A.mu_out + static_cast<size_t>(p) * PS)[i] = lam[p];
         }
     }
     if (A.bc_terms) warp_flush_wall(A.grad_wall, wall_h, gw);

@@ -732,10 +732,12 @@ __device__ __forceinline__ void row_block(const StepParams<S>& P, int rb, int ns
 #pragma unroll
             for (int p = 0; p < Q; ++p) {
                 if (ODD) {
-                    const int off = L::c(p, 0) + L::c(p, 1) * sy + L::c(p, 2) * sz;
-                    St::st(pop + static_cast<size_t>(p) * PS + (i + off), f[p]);
+                    // block-uniform base of direction p (plane p, shifted by c_p), indexed by i
+                    const long long off = static_cast<long long>(p) * static_cast<long long>(PS) + L::c(p, 0) +
+                                          L::c(p, 1) * sy + static_cast<long long>(L::c(p, 2)) * sz;
+                    St::st((pop + off) + i, f[p]);
                 } else {
-                    St::st(pop + static_cast<size_t>(inv<L>(p)) * PS + i, f[p]);
+                    St::st((pop + static_cast<size_t>(inv<L>(p)) * PS) + i, f[p]);
                 }
             }
         } else if constexpr (St::kShifted) {

@@ -160,6 +160,7 @@ struct Launch {
         AdjParams<T> a;
         a.flag = d.flag;
         a.link = d.link;
+        a.ltab = d.ltab;
         a.bc = d.bc;
         a.profile = d.profile;
         a.g = d.g;

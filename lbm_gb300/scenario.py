@@ -177,11 +177,14 @@ def taylor_green(n: int = 384, u0: float = 0.03, omega: float = 1.9, q: int = 19
     return s
 
 
-def taylor_green_velocity(n: int, u0: float) -> np.ndarray:
+def taylor_green_velocity(n: int, u0: float, z_slab=None) -> np.ndarray:
+    """u of the Taylor-Green vortex at the interior cells (z, y, x) (optionally only the z
+    indices in z_slab), cell centres at (i + 1/2) k."""
     k = 2 * np.pi / n
     c = (np.arange(n) + 0.5) * k
-    z, y, x = np.meshgrid(c, c, c, indexing="ij")
-    u = np.empty((n, n, n, 3))
+    cz = c if z_slab is None else c[z_slab]
+    z, y, x = np.meshgrid(cz, c, c, indexing="ij")
+    u = np.empty(z.shape + (3,))
     u[..., 0] = u0 * np.sin(x) * np.cos(y) * np.cos(z)
     u[..., 1] = -u0 * np.cos(x) * np.sin(y) * np.cos(z)
     u[..., 2] = 0.0
@@ -189,10 +192,17 @@ def taylor_green_velocity(n: int, u0: float) -> np.ndarray:
 
 
 def taylor_green_init(n: int, u0: float, q: int) -> np.ndarray:
+    """(Ng, Q) populations: feq(1, u_TG) in the interior, w_q in the ghost layer; built one z
+    slab at a time (the 384^3 box is 8.7 GB in FP64)."""
     m = _model.get(q)
-    f = np.tile(m.weights, ((n + 2) ** 3, 1))
-    feq = m.feq(np.ones((n, n, n)), taylor_green_velocity(n, u0))
-    f.reshape(n + 2, n + 2, n + 2, m.Q)[1:-1, 1:-1, 1:-1] = feq
+    f = np.empty(((n + 2) ** 3, m.Q))
+    f[:] = m.weights
+    f4 = f.reshape(n + 2, n + 2, n + 2, m.Q)
+    step = max(1, (1 << 22) // (n * n))
+    for z0 in range(0, n, step):
+        sl = slice(z0, min(n, z0 + step))
+        u = taylor_green_velocity(n, u0, sl)
+        f4[1 + sl.start:1 + sl.stop, 1:-1, 1:-1] = m.feq(np.ones(u.shape[:-1]), u)
     return f
 
 
