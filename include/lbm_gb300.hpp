@@ -281,7 +281,7 @@ class Domain {
     int phase{0};  // 0 idle, 1 after stream(), 2 after swap()
     mutable std::vector<Cell<M>> mirror;
     mutable bool mirror_valid{false};
-    bool mirror_dirty{false};
+    mutable bool mirror_dirty{false};
 
     void pull_mirror() const
     {
@@ -294,7 +294,7 @@ class Domain {
             for (size_t q = 0; q < M::Q; ++q) mirror[i][q] = f[i * M::Q + q];
         mirror_valid = true;
     }
-    void push_mirror()
+    void push_mirror() const
     {
         if (!mirror_dirty) return;
         const size_t n = mirror.size();
@@ -320,7 +320,26 @@ public:
     Domain(const Domain&) = delete;
     Domain& operator=(const Domain&) = delete;
 
-    lbm_domain* native() { return h; }
+    lbm_domain* native() const { return h; }
+
+    // Extension: solid cells (mask[z][y][x] of the interior, x fastest, nonzero = solid) bound to
+    // a new no-slip handler, as io::read_vtk_point_file does (vtk.hpp:135-150).
+    void set_solid_mask(const std::vector<std::uint8_t>& mask)
+    {
+        if (mask.size() != xl * yl * zl) throw std::logic_error("lbm_gb300: mask size must be xl*yl*zl");
+        push_mirror();
+        int handler = 0;
+        detail::check(lbm_set_solid_mask(h, mask.data(), &handler), h);
+        mirror_valid = false;
+    }
+    // Extension: density and velocity of the interior cells (x fastest), computed on the device.
+    void moments(std::vector<double>& rho, std::vector<double>& u) const
+    {
+        push_mirror();
+        rho.resize(xl * yl * zl);
+        u.resize(3 * xl * yl * zl);
+        detail::check(lbm_moments(h, rho.data(), u.data()), h);
+    }
 
     size_t xlength() const { return xl; }
     size_t ylength() const { return yl; }

@@ -17,6 +17,8 @@ CSRC = PKG / "csrc"
 LIBDIR = PKG / "_lib"
 OBJDIR = LIBDIR / "obj"
 LIB = LIBDIR / "liblbm_gb300.so"
+DRIVER_SRC = PKG / "driver" / "lbm_gb300_run.cpp"
+DRIVER = LIBDIR / "lbm_gb300_run"
 INCLUDE = PKG.parent / "include"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -76,7 +78,26 @@ def build(verbose: bool = False, out_dir: Path | None = None, defines: tuple = (
         res = subprocess.run(cmd, capture_output=True, text=True)
         if res.returncode != 0:
             raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")
+    if out_dir is None:
+        build_driver(lib)
     return lib
+
+
+def build_driver(lib: Path = LIB) -> Path:
+    """The C++ simulation driver (config file + XML scenario -> time loop -> VTS), linked against
+    the library next to it."""
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if cxx is None:
+        raise RuntimeError("a C++17 compiler (g++) is required for the driver")
+    deps = [DRIVER_SRC, INCLUDE / "lbm_gb300.hpp", INCLUDE / "lbm_gb300_io.hpp", INCLUDE / "lbm_gb300.h", lib]
+    if DRIVER.exists() and DRIVER.stat().st_mtime >= max(p.stat().st_mtime for p in deps):
+        return DRIVER
+    cmd = [cxx, "-std=c++17", "-O2", "-Wall", "-Wextra", "-I", str(INCLUDE), str(DRIVER_SRC), "-o", str(DRIVER),
+           "-L", str(lib.parent), "-llbm_gb300", "-Wl,-rpath,$ORIGIN"]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"driver build failed:\n{res.stdout}\n{res.stderr}")
+    return DRIVER
 
 
 if __name__ == "__main__":

@@ -1,0 +1,97 @@
+"""Scenarios read from XML / legacy-VTK files run on the GPU, bit for bit against the C port of
+the reference (FP64), and the VTS output of the device moments."""
+import xml.etree.ElementTree as ET
+
+import numpy as np
+import pytest
+
+import oracle
+from helpers import defined_entries
+from lbm_gb300 import BGKCollision, io
+from test_io import SHEAR_XML, STEP_XML, _decode, tube_mask, write_mask_vtk
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib(lbm_lib, oracle_built):
+    return lbm_lib
+
+
+def _check_vs_port(scn, steps):
+    from lbm_gb300 import build_domain
+    with build_domain(scn, "fp64") as dom:
+        dom.step(steps)
+        pops = dom.populations()
+    want = oracle.run_port(scn, steps)["pops"]
+    mask = defined_entries(scn)
+    assert np.array_equal(pops[mask], want[mask])
+
+
+@pytest.mark.parametrize("xml, steps", [(STEP_XML, 40), (SHEAR_XML, 35)])
+def test_xml_scenarios_fp64_vs_port(xml, steps):
+    _check_vs_port(io.parse_scenario(xml, q=19, tau=0.6), steps)
+
+
+def test_vtk_mask_scenario_fp64_vs_port(tmp_path):
+    write_mask_vtk(tmp_path / "tube.vtk", tube_mask(20, 11, 11, 4.2))
+    xml = ('<scenario name="Tube"><domain vtk-file="tube.vtk">'
+           '<boundary extent="z0" condition="noslip"/><boundary extent="zmax" condition="noslip"/>'
+           '<boundary extent="x0" condition="inflow" vx="0.03" vy="0" vz="0"/>'
+           '<boundary extent="xmax" condition="outflow"/><boundary extent="y0" condition="noslip"/>'
+           '<boundary extent="ymax" condition="noslip"/></domain></scenario>')
+    _check_vs_port(io.parse_scenario(xml, q=19, tau=0.6, base_dir=tmp_path), 30)
+
+
+def test_scenario_file_config_and_vts_output(tmp_path):
+    (tmp_path / "step.xml").write_text(STEP_XML)
+    cfg_file = tmp_path / "config.cfg"
+    cfg_file.write_text(f"tau = 0.6\ntimesteps = 20\ntimesteps-per-plot = 10\n"
+                        f"scenario-file = {tmp_path / 'step.xml'}\noutput-dir = {tmp_path / 'vtk'}\n")
+    cfg = io.Config([str(cfg_file)])
+    dom = io.parse_scenario_file(cfg.scenario_xml, cfg, BGKCollision(cfg.tau))
+    assert cfg.output_filename == "Backward step"
+    with dom:
+        for t in range(1, cfg.timesteps + 1):
+            dom.stream()
+            dom.swap()
+            dom.collide()
+            if t % cfg.timesteps_per_plot == 0:
+                path = io.write_vtk_file(dom, cfg.output_dir, cfg.output_filename, t)
+        rho, u = dom.moments()
+    assert path.name == "Backward step.20.vts"
+    arrays = {a.get("Name"): a for a in ET.fromstring(path.read_text()).iter("DataArray")}
+    assert np.array_equal(np.frombuffer(_decode(arrays["Density"]), "<f8"), rho.reshape(-1))
+    assert np.array_equal(np.frombuffer(_decode(arrays["Velocity"]), "<f8"), u.reshape(-1))
+    assert sorted(p.name for p in (tmp_path / "vtk").iterdir()) == ["Backward step.10.vts", "Backward step.20.vts"]
+
+
+def test_read_vtk_point_file_domain(tmp_path):
+    mask = tube_mask(10, 7, 6, 2.2)
+    write_mask_vtk(tmp_path / "m.vtk", mask, origin=(1.0, 2.0, 3.0), spacing=(0.5, 0.5, 0.5))
+    with io.read_vtk_point_file(tmp_path / "m.vtk", BGKCollision(0.7)) as dom:
+        assert (dom.xl, dom.yl, dom.zl) == (10, 7, 6)
+        assert (dom.xo, dom.yo, dom.zo, dom.xs) == (1.0, 2.0, 3.0, 0.5)
+        dom.step(3)
+        rho, _ = dom.moments()
+    # solid cells read back as rest density (no fluid populations are ever written there)
+    assert np.all(np.isfinite(rho[mask == 1]))
+
+
+def test_driver_run_matches_python_path(tmp_path):
+    import subprocess
+    from lbm_gb300 import _build, build_domain
+    drv = _build.build_driver()
+    (tmp_path / "step.xml").write_text(STEP_XML)
+    (tmp_path / "config.cfg").write_text("tau = 0.6\ntimesteps = 24\ntimesteps-per-plot = 12\n"
+                                         "scenario-file = step.xml\noutput-dir = vtk\n")
+    r = subprocess.run([str(drv), "config.cfg"], capture_output=True, text=True, cwd=tmp_path, timeout=120)
+    assert r.returncode == 0, r.stderr
+    assert "MLUPS" in r.stdout
+    vts = tmp_path / "vtk" / "Backward step.24.vts"
+    arrays = {a.get("Name"): a for a in ET.fromstring(vts.read_text()).iter("DataArray")}
+    with build_domain(io.parse_scenario(STEP_XML, q=19, tau=0.6), "fp64") as dom:
+        dom.step(24)
+        rho, u = dom.moments()
+    assert np.array_equal(np.frombuffer(_decode(arrays["Density"]), "<f8"), rho.reshape(-1))
+    assert np.array_equal(np.frombuffer(_decode(arrays["Velocity"]), "<f8"), u.reshape(-1))
