@@ -517,7 +517,7 @@ constexpr size_t row_smem_bytes()
     return kSegs * stage_bytes<L, S>() + link_smem_bytes<S>();
 }
 
-template <class L, class S, bool ODD>
+template <class L, class S, bool ODD, bool INSTR>
 __device__ __forceinline__ void edge_block(const StepParams<S>& P, int blk, unsigned char* smem_raw)
 {
     using St = Store<S>;
@@ -546,7 +546,7 @@ __device__ __forceinline__ void edge_block(const StepParams<S>& P, int blk, unsi
             }
         }
         collide_any<L, S>(f, P, m);
-        if (P.rec) record_moments<S>(P.rec, i, m);
+        if (INSTR && P.rec) record_moments<S>(P.rec, i, m);
         store_edge_populations<L, S, ODD>(P, x, y, z, i, f);
         if (link & ((1u << Q) - 1u)) {
             T* fs = reinterpret_cast<T*>(smem_raw) + tx;
@@ -555,7 +555,7 @@ __device__ __forceinline__ void edge_block(const StepParams<S>& P, int blk, unsi
             store_handler_values<L, S, ODD>(P, x, y, z, i, link, fs, kRowCells);
         }
     }
-    if (P.mon) monitor_add<S>(P.mon, m, j < P.n_edge);
+    if (INSTR && P.mon) monitor_add<S>(P.mon, m, j < P.n_edge);
 }
 
 __device__ __forceinline__ void segment_origin(const Geom& g, int seg, const FastDiv& dx, const FastDiv& dy, int& x0,
@@ -639,7 +639,7 @@ __device__ __forceinline__ V opaque(V v)
     return v;
 }
 
-template <class L, class S, bool ODD>
+template <class L, class S, bool ODD, bool INSTR>
 __device__ __forceinline__ void row_block(const StepParams<S>& P, int rb, int nseg, const FastDiv& dx, const FastDiv& dy,
                                           unsigned char* smem_raw, uint64_t* bars)
 {
@@ -722,28 +722,38 @@ __device__ __forceinline__ void row_block(const StepParams<S>& P, int rb, int ns
 #pragma unroll
             for (int q = 0; q < Q; ++q) f[q] = St::ld(buf + q * W + PAD + tx - (ODD ? L::c(q, 0) : 0));
             collide_any<L, S>(f, P, m);
-            if (P.rec) record_moments<S>(P.rec, i, m);
+            if (INSTR && P.rec) record_moments<S>(P.rec, i, m);
             if (wl) {
                 if constexpr (St::kShifted) {
                     if (rec) cp_async_wait_all();
                 }
                 link_values<L, S, ODD>(P, i, f, m, wl, rec, opaque(PS), opaque(sy));
             }
+            // stores plane by plane through one running pointer: each step adds a block-uniform
+            // delta (the plane stride, and on odd steps the change of the shift c_p)
+            if (ODD) {
+                S* ptr = pop + i + (L::c(0, 0) + L::c(0, 1) * sy + L::c(0, 2) * sz);
 #pragma unroll
-            for (int p = 0; p < Q; ++p) {
-                if (ODD) {
-                    // block-uniform base of direction p (plane p, shifted by c_p), indexed by i
-                    const long long off = static_cast<long long>(p) * static_cast<long long>(PS) + L::c(p, 0) +
-                                          L::c(p, 1) * sy + static_cast<long long>(L::c(p, 2)) * sz;
-                    St::st((pop + off) + i, f[p]);
-                } else {
-                    St::st((pop + static_cast<size_t>(inv<L>(p)) * PS) + i, f[p]);
+                for (int p = 0; p < Q; ++p) {
+                    St::st(ptr, f[p]);
+                    if (p + 1 < Q) {
+                        const int d = (L::c(p + 1, 0) - L::c(p, 0)) + (L::c(p + 1, 1) - L::c(p, 1)) * sy +
+                                      (L::c(p + 1, 2) - L::c(p, 2)) * sz;
+                        ptr += static_cast<long long>(PS) + d;
+                    }
+                }
+            } else {
+                S* ptr = pop + i;
+#pragma unroll
+                for (int k = 0; k < Q; ++k) {
+                    St::st(ptr, f[inv<L>(k)]);
+                    if (k + 1 < Q) ptr += PS;
                 }
             }
         } else if constexpr (St::kShifted) {
             if (rec) cp_async_wait_all();  // no copy may still be landing when the block ends
         }
-        if (P.mon) monitor_add<S>(P.mon, m, bulk);
+        if (INSTR && P.mon) monitor_add<S>(P.mon, m, bulk);
     }
 }
 
@@ -776,7 +786,9 @@ constexpr int min_blocks()
 #define LBMG_EDGE_SPAN 0.6
 #endif
 constexpr double kEdgeSpan = LBMG_EDGE_SPAN;
-template <class L, class S, bool ODD>
+// INSTR: the step monitor and the adjoint's record may be active (P.mon / P.rec are tested);
+// plain steps are compiled without them.
+template <class L, class S, bool ODD, bool INSTR>
 __global__ void __launch_bounds__(kRowCells, min_blocks<L, S, ODD>())
     step_kernel(const StepParams<S> P, int n_edge_blocks, FastDiv edge_stride, int nseg, FastDiv nseg_x, FastDiv yl)
 {
@@ -786,11 +798,11 @@ __global__ void __launch_bounds__(kRowCells, min_blocks<L, S, ODD>())
     const int interleaved = n_edge_blocks * static_cast<int>(edge_stride.d);
     const int e = static_cast<int>(fast_div(static_cast<uint32_t>(b), edge_stride));
     if (b < interleaved && b == e * static_cast<int>(edge_stride.d))
-        edge_block<L, S, ODD>(P, e, smem_raw);
+        edge_block<L, S, ODD, INSTR>(P, e, smem_raw);
     else if (b < interleaved)
-        row_block<L, S, ODD>(P, b - (e + 1), nseg, nseg_x, yl, smem_raw, bars);
+        row_block<L, S, ODD, INSTR>(P, b - (e + 1), nseg, nseg_x, yl, smem_raw, bars);
     else
-        row_block<L, S, ODD>(P, b - n_edge_blocks, nseg, nseg_x, yl, smem_raw, bars);
+        row_block<L, S, ODD, INSTR>(P, b - n_edge_blocks, nseg, nseg_x, yl, smem_raw, bars);
 }
 
 // ------------------------------------------------------------------------------------------

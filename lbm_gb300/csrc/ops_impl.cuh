@@ -93,17 +93,16 @@ struct Launch {
         if constexpr (smem > 48 * 1024) {
             static bool opted_in = false;
             if (!opted_in) {
-                cudaFuncSetAttribute(step_kernel<L, S, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     static_cast<int>(smem));
-                cudaFuncSetAttribute(step_kernel<L, S, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     static_cast<int>(smem));
+                for (auto k : {step_kernel<L, S, true, false>, step_kernel<L, S, false, false>,
+                               step_kernel<L, S, true, true>, step_kernel<L, S, false, true>})
+                    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
                 opted_in = true;
             }
         }
-        if (t & 1)
-            step_kernel<L, S, true><<<blocks, kRowCells, smem, s>>>(p, n_edge_blocks, fes, nseg, fx, fy);
-        else
-            step_kernel<L, S, false><<<blocks, kRowCells, smem, s>>>(p, n_edge_blocks, fes, nseg, fx, fy);
+        const bool instr = mon_out != nullptr || rec != nullptr;
+        auto* k = (t & 1) ? (instr ? step_kernel<L, S, true, true> : step_kernel<L, S, true, false>)
+                          : (instr ? step_kernel<L, S, false, true> : step_kernel<L, S, false, false>);
+        k<<<blocks, kRowCells, smem, s>>>(p, n_edge_blocks, fes, nseg, fx, fy);
         if (mon_out) monitor_final_kernel<<<1, 256, 0, s>>>(d.mon, mon_out);
         side_passes(d, t, s);
     }
