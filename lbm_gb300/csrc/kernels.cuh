@@ -27,6 +27,7 @@ struct Store<double> {
     static constexpr bool kShifted = false;
     __device__ static __forceinline__ double ld(const double* p) { return *p; }
     __device__ static __forceinline__ void st(double* p, double v) { *p = v; }
+    __device__ static __forceinline__ void st_stream(double* p, double v) { __stcs(p, v); }
 };
 template <>
 struct Store<float> {
@@ -34,6 +35,7 @@ struct Store<float> {
     static constexpr bool kShifted = true;
     __device__ static __forceinline__ float ld(const float* p) { return *p; }
     __device__ static __forceinline__ void st(float* p, float v) { *p = v; }
+    __device__ static __forceinline__ void st_stream(float* p, float v) { __stcs(p, v); }
 };
 template <>
 struct Store<__half> {
@@ -41,6 +43,11 @@ struct Store<__half> {
     static constexpr bool kShifted = true;
     __device__ static __forceinline__ float ld(const __half* p) { return __half2float(*p); }
     __device__ static __forceinline__ void st(__half* p, float v) { *p = __float2half_rn(v); }
+    __device__ static __forceinline__ void st_stream(__half* p, float v)
+    {
+        const unsigned short b = __half_as_ushort(__float2half_rn(v));
+        asm volatile("st.global.cs.b16 [%0], %1;" ::"l"(p), "h"(b) : "memory");
+    }
 };
 template <>
 struct Store<__nv_bfloat16> {
@@ -53,6 +60,11 @@ struct Store<__nv_bfloat16> {
     __device__ static __forceinline__ void st(__nv_bfloat16* p, float v)
     {
         *p = __float2bfloat16_rn(v);
+    }
+    __device__ static __forceinline__ void st_stream(__nv_bfloat16* p, float v)
+    {
+        const unsigned short b = __bfloat16_as_ushort(__float2bfloat16_rn(v));
+        asm volatile("st.global.cs.b16 [%0], %1;" ::"l"(p), "h"(b) : "memory");
     }
 };
 
@@ -678,7 +690,7 @@ __device__ __forceinline__ void row_block(const StepParams<S>& P, int rb, int ns
                 const S* src = pop + static_cast<size_t>(plane) * PS +
                                (static_cast<size_t>(kXOff + x0 - PAD) +
                                 static_cast<size_t>(P.g.XS) * (static_cast<size_t>(ry) + static_cast<size_t>(P.g.YS) * rz));
-                bulk_g2s(reinterpret_cast<S*>(smem_raw + s * SB) + q * W, src, bytes, &bars[s]);
+                bulk_g2s_hint(reinterpret_cast<S*>(smem_raw + s * SB) + q * W, src, bytes, &bars[s], l2_evict_first());
             }
         }
     }
@@ -735,7 +747,7 @@ __device__ __forceinline__ void row_block(const StepParams<S>& P, int rb, int ns
                 S* ptr = pop + i + (L::c(0, 0) + L::c(0, 1) * sy + L::c(0, 2) * sz);
 #pragma unroll
                 for (int p = 0; p < Q; ++p) {
-                    St::st(ptr, f[p]);
+                    St::st_stream(ptr, f[p]);
                     if (p + 1 < Q) {
                         const int d = (L::c(p + 1, 0) - L::c(p, 0)) + (L::c(p + 1, 1) - L::c(p, 1)) * sy +
                                       (L::c(p + 1, 2) - L::c(p, 2)) * sz;
@@ -746,7 +758,7 @@ __device__ __forceinline__ void row_block(const StepParams<S>& P, int rb, int ns
                 S* ptr = pop + i;
 #pragma unroll
                 for (int k = 0; k < Q; ++k) {
-                    St::st(ptr, f[inv<L>(k)]);
+                    St::st_stream(ptr, f[inv<L>(k)]);
                     if (k + 1 < Q) ptr += PS;
                 }
             }
