@@ -139,20 +139,20 @@ __global__ void __launch_bounds__(kBlockX) adjoint_step_kernel(const AdjParams<T
             for (int p = 0; p < Q; ++p) {
                 const long long off = static_cast<long long>(p) * static_cast<long long>(PS) + L::c(p, 0) +
                                       L::c(p, 1) * A.g.XS + static_cast<long long>(L::c(p, 2)) * A.g.XS * A.g.YS;
-                lam[p] = (A.mu_in + off)[i];
+                lam[p] = __ldcs(&(A.mu_in + off)[i]);
             }
         } else {
 #pragma unroll
             for (int p = 0; p < Q; ++p) {
                 int mx, my, mz;
                 nbr_xyz(A.g, x, y, z, L::c(p, 0), L::c(p, 1), L::c(p, 2), mx, my, mz);
-                lam[p] = A.mu_in[static_cast<size_t>(p) * PS + cidx(A.g, mx, my, mz)];
+                lam[p] = __ldcs(&A.mu_in[static_cast<size_t>(p) * PS + cidx(A.g, mx, my, mz)]);
             }
         }
-        const T rho_s = A.rec[4 * static_cast<size_t>(i) + 0];
-        const T jxs = A.rec[4 * static_cast<size_t>(i) + 1];
-        const T jys = A.rec[4 * static_cast<size_t>(i) + 2];
-        const T jzs = A.rec[4 * static_cast<size_t>(i) + 3];
+        const T rho_s = __ldcs(&A.rec[4 * static_cast<size_t>(i) + 0]);
+        const T jxs = __ldcs(&A.rec[4 * static_cast<size_t>(i) + 1]);
+        const T jys = __ldcs(&A.rec[4 * static_cast<size_t>(i) + 2]);
+        const T jzs = __ldcs(&A.rec[4 * static_cast<size_t>(i) + 3]);
         const uint2 lw = fl != kFluidBulk ? A.link[i] : make_uint2(0u, kNoRecord);
         const uint32_t link = lw.x;
         // links whose handler needs its table entry: every link of a kFluidEdge cell; of a
@@ -238,7 +238,7 @@ __global__ void __launch_bounds__(kBlockX) adjoint_step_kernel(const AdjParams<T
         if (A.write_mu) {
             bgk_adjoint<L, T>(lam, rho_s, jxs, jys, jzs, A.omega);
 #pragma unroll
-            for (int p = 0; p < Q; ++p) (A.mu_out + static_cast<size_t>(p) * PS)[i] = lam[p];
+            for (int p = 0; p < Q; ++p) __stcs(&(A.mu_out + static_cast<size_t>(p) * PS)[i], lam[p]);
         }
     }
     if (A.bc_terms) warp_flush_wall(A.grad_wall, wall_h, gw);

@@ -382,10 +382,10 @@ template <class S>
 __device__ __forceinline__ void record_moments(typename Store<S>::C* rec, int i, const typename Store<S>::C (&m)[4])
 {
     using T = typename Store<S>::C;
-    rec[4 * static_cast<size_t>(i) + 0] = Store<S>::kShifted ? T(1) + m[0] : m[0];
-    rec[4 * static_cast<size_t>(i) + 1] = m[1];
-    rec[4 * static_cast<size_t>(i) + 2] = m[2];
-    rec[4 * static_cast<size_t>(i) + 3] = m[3];
+    __stcs(&rec[4 * static_cast<size_t>(i) + 0], Store<S>::kShifted ? T(1) + m[0] : m[0]);
+    __stcs(&rec[4 * static_cast<size_t>(i) + 1], m[1]);
+    __stcs(&rec[4 * static_cast<size_t>(i) + 2], m[2]);
+    __stcs(&rec[4 * static_cast<size_t>(i) + 3], m[3]);
 }
 
 // Adds the warp's totals of m (the moments collide_any returned; zeros for a thread without a
