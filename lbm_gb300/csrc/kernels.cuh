@@ -771,9 +771,17 @@ __device__ __forceinline__ void row_block(const StepParams<S>& P, int rb, int ns
 
 // Resident blocks per SM that the register allocation of a step kernel must allow (0: no
 // bound; ptxas then picks fewer registers than with an explicit 1). Unbounded, the shifted
-// D3Q19 kernels take 56 registers (9 blocks per SM); bounded to 10 blocks they keep 48. FP64 is
-// never bounded. LBMG_MINB_EVEN / LBMG_MINB_ODD override the shifted-storage
+// D3Q19 kernels take 56 registers (9 blocks per SM); bounded to 10 blocks they keep 48, and so do
+// the D3Q15 ones (one odd-step spill of 4 bytes, 2% faster than 56 registers). D3Q27 gains
+// nothing from a bound; FP64 is never bounded. LBMG_MINB_Q15 / LBMG_MINB_Q27 set the D3Q15 and
+// D3Q27 values in tuning builds. LBMG_MINB_EVEN / LBMG_MINB_ODD override the shifted-storage
 // values in tuning builds.
+#ifndef LBMG_MINB_Q15
+#define LBMG_MINB_Q15 10
+#endif
+#ifndef LBMG_MINB_Q27
+#define LBMG_MINB_Q27 0
+#endif
 template <class L, class S, bool ODD>
 constexpr int min_blocks()
 {
@@ -786,7 +794,7 @@ constexpr int min_blocks()
 #if defined(LBMG_MINB_EVEN)
         if (!ODD) return LBMG_MINB_EVEN;
 #endif
-        return L::Q == 19 ? 10 : 0;
+        return L::Q == 19 ? 10 : L::Q == 27 ? LBMG_MINB_Q27 : LBMG_MINB_Q15;
     }
 }
 
