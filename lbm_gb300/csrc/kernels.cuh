@@ -638,6 +638,35 @@ __device__ __forceinline__ void link_values(const StepParams<S>& P, int i, typen
     }
 }
 
+// The Q bulk stores of a row-block cell at layout pointer `cell`, plane by plane through one
+// running pointer (each step adds a block-uniform delta: the plane stride and, on odd steps, the
+// change of the shift c_p).
+template <class L, class S, bool ODD, bool STREAM>
+__device__ __forceinline__ void store_cell(S* cell, const typename Store<S>::C (&f)[L::Q], size_t PS, int sy, int sz)
+{
+    using St = Store<S>;
+    constexpr int Q = L::Q;
+    if (ODD) {
+        S* ptr = cell + (L::c(0, 0) + L::c(0, 1) * sy + L::c(0, 2) * sz);
+#pragma unroll
+        for (int p = 0; p < Q; ++p) {
+            if (STREAM) St::st_stream(ptr, f[p]); else St::st(ptr, f[p]);
+            if (p + 1 < Q) {
+                const int d = (L::c(p + 1, 0) - L::c(p, 0)) + (L::c(p + 1, 1) - L::c(p, 1)) * sy +
+                              (L::c(p + 1, 2) - L::c(p, 2)) * sz;
+                ptr += static_cast<long long>(PS) + d;
+            }
+        }
+    } else {
+        S* ptr = cell;
+#pragma unroll
+        for (int k = 0; k < Q; ++k) {
+            if (STREAM) St::st_stream(ptr, f[inv<L>(k)]); else St::st(ptr, f[inv<L>(k)]);
+            if (k + 1 < Q) ptr += PS;
+        }
+    }
+}
+
 // The value v, hidden from the optimiser: address arithmetic that uses it stays inside the
 // (rarely taken) branch it is written in instead of being hoisted into registers held by every
 // thread of the kernel.
@@ -690,7 +719,8 @@ __device__ __forceinline__ void row_block(const StepParams<S>& P, int rb, int ns
                 const S* src = pop + static_cast<size_t>(plane) * PS +
                                (static_cast<size_t>(kXOff + x0 - PAD) +
                                 static_cast<size_t>(P.g.XS) * (static_cast<size_t>(ry) + static_cast<size_t>(P.g.YS) * rz));
-                bulk_g2s_hint(reinterpret_cast<S*>(smem_raw + s * SB) + q * W, src, bytes, &bars[s], l2_evict_first());
+                bulk_g2s_hint(reinterpret_cast<S*>(smem_raw + s * SB) + q * W, src, bytes, &bars[s],
+                              l2_stream_policy(P.n_edge == 0));
             }
         }
     }
@@ -742,26 +772,12 @@ __device__ __forceinline__ void row_block(const StepParams<S>& P, int rb, int ns
                 link_values<L, S, ODD>(P, i, f, m, wl, rec, opaque(PS), opaque(sy));
             }
             // stores plane by plane through one running pointer: each step adds a block-uniform
-            // delta (the plane stride, and on odd steps the change of the shift c_p)
-            if (ODD) {
-                S* ptr = pop + i + (L::c(0, 0) + L::c(0, 1) * sy + L::c(0, 2) * sz);
-#pragma unroll
-                for (int p = 0; p < Q; ++p) {
-                    St::st_stream(ptr, f[p]);
-                    if (p + 1 < Q) {
-                        const int d = (L::c(p + 1, 0) - L::c(p, 0)) + (L::c(p + 1, 1) - L::c(p, 1)) * sy +
-                                      (L::c(p + 1, 2) - L::c(p, 2)) * sz;
-                        ptr += static_cast<long long>(PS) + d;
-                    }
-                }
-            } else {
-                S* ptr = pop + i;
-#pragma unroll
-                for (int k = 0; k < Q; ++k) {
-                    St::st_stream(ptr, f[inv<L>(k)]);
-                    if (k + 1 < Q) ptr += PS;
-                }
-            }
+            // delta (the plane stride, and on odd steps the change of the shift c_p). Streaming
+            // (evict-first) stores when every cell is a row-block cell (see l2_stream_policy).
+            if (P.n_edge == 0)
+                store_cell<L, S, ODD, true>(pop + i, f, PS, sy, sz);
+            else
+                store_cell<L, S, ODD, false>(pop + i, f, PS, sy, sz);
         } else if constexpr (St::kShifted) {
             if (rec) cp_async_wait_all();  // no copy may still be landing when the block ends
         }

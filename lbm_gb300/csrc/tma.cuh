@@ -38,12 +38,17 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t by
 
 // Global -> shared bulk copy of `bytes` (multiple of 16, both addresses 16-byte aligned),
 // completing on `bar`.
-// L2 policy for data read once per step (the streamed populations): evict first, so that the
-// small per-cell arrays (flags, link entries, handler records) stay in L2 between steps.
-__device__ __forceinline__ uint64_t l2_evict_first()
+// L2 policy for the streamed populations. Evict first keeps the small per-cell arrays (flags,
+// link entries, handler records) in L2 between steps; it is used when every cell is updated by a
+// row block. Edge blocks re-read rows that row blocks have just streamed, so domains with edge
+// cells keep the normal policy.
+__device__ __forceinline__ uint64_t l2_stream_policy(bool evict_first)
 {
     uint64_t pol;
-    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+    if (evict_first)
+        asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+    else
+        asm volatile("createpolicy.fractional.L2::evict_normal.b64 %0, 1.0;" : "=l"(pol));
     return pol;
 }
 
