@@ -192,7 +192,7 @@ def test_bad_arguments_on_device():
 
 # ------------------------------------------------------------------------------------------
 # Reduced precision: FP32 arithmetic on shifted FP32 / FP16 / BF16 storage against FP64.
-# Tolerances (relative L2 over interior fluid cells) are stated here and in the design doc.
+# Tolerances: relative L2 over interior fluid cells, stated below.
 # ------------------------------------------------------------------------------------------
 TOL_U = {"fp32": 5e-6, "fp16": 2e-3, "bf16": 2e-2}
 TOL_RHO = {"fp32": 2e-7, "fp16": 5e-5, "bf16": 5e-4}

@@ -14,7 +14,9 @@ import pytest
 from lbm_gb300 import io
 from lbm_gb300 import scenario as S
 
-REF_SCEN = Path("/root/reference/build/scenarios")
+from oracle.checkers import REF_DIR
+
+REF_SCEN = REF_DIR / "build" / "scenarios"
 
 STEP_XML = """<?xml version="1.0" ?>
 <scenario name="Backward step">
