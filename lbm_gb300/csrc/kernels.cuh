@@ -477,21 +477,23 @@ __device__ __forceinline__ void store_edge_populations(const StepParams<S>& P, i
 
 // The step kernel, one launch per time step, with two kinds of blocks.
 //
-// Edge blocks are interleaved with the row blocks (see step_kernel), so that their
-// latency-bound work overlaps the streaming of the row blocks. Each updates up to
-// kRowCells edge cells (fluid cells next to a non-fluid cell or a periodic wrap) from the sorted
-// list P.edge, one per thread, through global memory: pulls from the wrapped neighbours or from
-// the boundary slots, stores through store_edge_populations and store_handler_values (the
-// post-collision populations go through shared memory, where the handler loop reads them).
+// Row blocks update the bulk and wall cells (kFluidBulk, kFluidWall) of kSegs consecutive
+// segments of kRowCells cells of x-rows, one thread per cell:
+// - At the start the first warp brings the Q source rows of every segment into the segment's own
+//   shared-memory stage with bulk asynchronous copies (TMA), one copy per lane, each stage
+//   completing on its own mbarrier. Each copied row is the segment widened by 16 bytes on both
+//   sides, which keeps source and size 16-byte aligned and covers the +-1 shift in x of the
+//   odd-step pulls. The loads in flight are bounded by shared memory rather than registers.
+// - While the rows land, each thread loads its flag and link entry and, for a cell with a
+//   LinkRecord, copies the record into shared memory.
+// - Each cell then collides from the stage, writes the handler values of its links
+//   (link_values) and stores its Q populations (store_cell). Handler values sit where the next
+//   step pulls them, so no cell needs a special load.
 //
-// Row blocks update the bulk cells of kSegs consecutive segments of kRowCells cells of x-rows,
-// one thread per cell. At the start the first warp brings the Q source rows of every segment into
-// its own shared-memory stage with bulk asynchronous copies (TMA), one copy per lane, each stage
-// completing on its own mbarrier; the block then collides the segments in order, the later
-// copies landing while the earlier segments compute. The loads in flight are bounded by shared
-// memory rather than registers. Each copied row is the segment widened by 16 bytes on both
-// sides, which keeps source and size 16-byte aligned and covers the +-1 shift in x of the
-// odd-step pulls.
+// Edge blocks take the cells a row block cannot: a periodic wrap, a free-slip or ghost-fluid
+// neighbour, or more handler constants than a record holds. They work from the sorted list
+// P.edge, one cell per thread, through global memory (wrapped pulls, store_edge_populations,
+// store_handler_values), and are spread over the first part of the grid (see step_kernel).
 #ifndef LBMG_ROW_CELLS
 #define LBMG_ROW_CELLS 128
 #endif
