@@ -135,11 +135,17 @@ __global__ void __launch_bounds__(kBlockX) adjoint_step_kernel(const AdjParams<T
         // every adjoint array (cleared once, never written), so no neighbour test is needed; bulk
         // cells have no wrapped neighbour either.
         if (fl != kFluidEdge) {  // no wrapped neighbour
+            // one running pointer over the planes (block-uniform deltas), as the step's stores
+            const int sy = A.g.XS, sz = A.g.XS * A.g.YS;
+            const T* ptr = A.mu_in + i + (L::c(0, 0) + L::c(0, 1) * sy + L::c(0, 2) * sz);
 #pragma unroll
             for (int p = 0; p < Q; ++p) {
-                const long long off = static_cast<long long>(p) * static_cast<long long>(PS) + L::c(p, 0) +
-                                      L::c(p, 1) * A.g.XS + static_cast<long long>(L::c(p, 2)) * A.g.XS * A.g.YS;
-                lam[p] = __ldcs(&(A.mu_in + off)[i]);
+                lam[p] = __ldcs(ptr);
+                if (p + 1 < Q) {
+                    const int d = (L::c(p + 1, 0) - L::c(p, 0)) + (L::c(p + 1, 1) - L::c(p, 1)) * sy +
+                                  (L::c(p + 1, 2) - L::c(p, 2)) * sz;
+                    ptr += static_cast<long long>(PS) + d;
+                }
             }
         } else {
 #pragma unroll
@@ -237,8 +243,12 @@ __global__ void __launch_bounds__(kBlockX) adjoint_step_kernel(const AdjParams<T
         }
         if (A.write_mu) {
             bgk_adjoint<L, T>(lam, rho_s, jxs, jys, jzs, A.omega);
+            T* out = A.mu_out + i;
 #pragma unroll
-            for (int p = 0; p < Q; ++p) __stcs(&(A.mu_out + static_cast<size_t>(p) * PS)[i], lam[p]);
+            for (int p = 0; p < Q; ++p) {
+                __stcs(out, lam[p]);
+                out += PS;
+            }
         }
     }
     if (A.bc_terms) warp_flush_wall(A.grad_wall, wall_h, gw);
