@@ -295,8 +295,15 @@ __device__ __forceinline__ void collide_shifted(float (&s)[L::Q], float omega, f
         const float sym = fmaf(cu * cu, rB, base);
         const float asym = cu * rA;
         const float w = static_cast<float>(L::w(q));
-        s[q] = fmaf(omega, fmaf(w, sym + asym, -s[q]), s[q]);
-        s[L::Q - 1 - q] = fmaf(omega, fmaf(w, sym - asym, -s[L::Q - 1 - q]), s[L::Q - 1 - q]);
+        // the pair (q, inv q) in one packed FP32x2 FMA chain: each lane performs the operations
+        // fmaf(omega, fmaf(w, sym +- asym, -s), s) exactly as written for one population
+        const int qb = L::Q - 1 - q;
+        const float2 e = make_float2(sym + asym, sym - asym);
+        const float2 sv = make_float2(s[q], s[qb]);
+        const float2 t = __ffma2_rn(make_float2(w, w), e, make_float2(-sv.x, -sv.y));
+        const float2 r = __ffma2_rn(make_float2(omega, omega), t, sv);
+        s[q] = r.x;
+        s[qb] = r.y;
     }
 }
 
