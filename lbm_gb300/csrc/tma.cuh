@@ -22,13 +22,6 @@ __device__ __forceinline__ void fence_mbar_init()
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
 
-// Orders this thread's earlier generic-proxy accesses to shared memory before later async-proxy
-// (TMA) accesses.
-__device__ __forceinline__ void fence_proxy_async_smem()
-{
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-}
-
 // Arrive once and announce `bytes` of incoming transactions on the barrier.
 __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes)
 {
@@ -36,8 +29,6 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t by
                  : "memory");
 }
 
-// Global -> shared bulk copy of `bytes` (multiple of 16, both addresses 16-byte aligned),
-// completing on `bar`.
 // L2 policy for the streamed populations. Evict first keeps the small per-cell arrays (flags,
 // link entries, handler records) in L2 between steps; it is used when every cell is updated by a
 // row block. Edge blocks re-read rows that row blocks have just streamed, so domains with edge
@@ -52,21 +43,14 @@ __device__ __forceinline__ uint64_t l2_stream_policy(bool evict_first)
     return pol;
 }
 
+// Global -> shared bulk copy of `bytes` (multiple of 16, both addresses 16-byte aligned),
+// completing on `bar`, with L2 cache policy `pol`.
 __device__ __forceinline__ void bulk_g2s_hint(void* dst, const void* src, uint32_t bytes, uint64_t* bar, uint64_t pol)
 {
     asm volatile(
         "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::"r"(
             smem_u32(dst)),
         "l"(src), "r"(bytes), "r"(smem_u32(bar)), "l"(pol)
-        : "memory");
-}
-
-__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar)
-{
-    asm volatile(
-        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-            smem_u32(dst)),
-        "l"(src), "r"(bytes), "r"(smem_u32(bar))
         : "memory");
 }
 
