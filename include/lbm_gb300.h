@@ -159,8 +159,8 @@ int lbm_adjoint_objective_ke(lbm_domain* d, const int64_t box[6], double* J);
  * upstream gradient when wrapped in an autodiff framework), with the state the run started from
  * held fixed. That state includes the boundary values its first step pulls (computed by the step
  * before it, as in the reference), so theta acts through the run's steps 2 .. n. Recomputes each
- * checkpoint segment
- * while recording per-cell mass and momentum, then runs the adjoint steps backwards through it.
+ * checkpoint segment while recording per-cell mass and momentum, then runs the adjoint steps
+ * backwards through it.
  * grad_inflow (may be NULL): 3 doubles per cell over all cells (reference cell order), the
  * gradient with respect to the inflow velocity of each inflow cell (the per-cell profile or the
  * handler's uniform velocity at that cell); grad_wall (may be NULL): 3 doubles per handler id
