@@ -157,7 +157,7 @@ def run_ours(args, rank, world, local):
     import torch
     import torch.distributed as dist
 
-    from lbm_gb300 import build_domain, capi
+    from lbm_gb300 import build_domain
     torch.cuda.set_device(local)
     size = tuple(int(v) for v in args.size.split(","))
     K, W = args.steps, args.warmup
@@ -266,29 +266,13 @@ def run_adjoint(xl=128, yl=64, zl=64, steps=2000, ckpt=100):
     energy in x in [96, 128) (interior cells 97..128). FP32 forward + adjoint; plain FP32 steps timed
     beside it; the FP32 and FP64 adjoint gradients at three inlet cells against FP64 central finite
     differences (h = 1e-5)."""
-    import torch
     from lbm_gb300 import build_domain
     from lbm_gb300 import scenario as S
     scn = S.adjoint_channel(xl, yl, zl, omega=1.7, seed=0)
     box = (97, xl, 1, yl, 1, zl)
-
-    def timed(fn):
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        r = fn()
-        torch.cuda.synchronize()
-        return time.perf_counter() - t0, r
-
     with build_domain(scn, "fp32") as d:
         plain = time_steps(d, steps, 5)
-    with build_domain(scn, "fp32") as d:
-        d.step(0)
-        d.sync()
-        fwd, _ = timed(lambda: (d.adjoint_forward(steps, ckpt), d.sync()))
-        J32 = d.objective_ke(box)
-        bwd, (g32, _) = timed(lambda: d.adjoint_backward(box))
-        bwd2, _ = timed(lambda: d.adjoint_backward(box))  # allocations warm
-    bwd = min(bwd, bwd2)
+    cost, (J32, (g32, _)) = _adjoint_costs(scn, "fp32", steps, ckpt, box)
     with build_domain(scn, "fp64") as d:
         d.adjoint_forward(steps, ckpt)
         J64 = d.objective_ke(box)
@@ -316,17 +300,62 @@ def run_adjoint(xl=128, yl=64, zl=64, steps=2000, ckpt=100):
                     f"{steps} steps, checkpoint every {ckpt}, J = KE in x in [96,{xl})",
         "storage": "fp32 (f - w)", "steps": steps, "ckpt_every": ckpt,
         "forward_plain_ms_per_step": plain / steps * 1e3,
-        "forward_ckpt_ms_per_step": fwd / steps * 1e3,
-        "backward_ms_per_step": bwd / steps * 1e3,
-        "backward_over_forward": bwd / plain,
-        "forward_plus_backward_over_forward": (fwd + bwd) / plain,
+        **_adjoint_report(cost, plain / steps),
         "forward_mlups": n * steps / plain / 1e6,
         "J_fp32": J32, "J_fp64": J64,
         "fd_check": {"param": "inlet u_x at (y, z)", "cells": cells, "fd_fp64": fds,
                      "max_rel_err_fp32_adjoint": max(errs32), "max_rel_err_fp64_adjoint": max(errs64),
                      "h": h},
-        "timing": "wall clock around synchronised calls (backward includes its allocations and the "
-                  "gradient download); plain steps by CUDA events",
+    }
+
+
+def _adjoint_costs(scn, prec, steps, ckpt, box):
+    """Wall-clock seconds of adjoint_forward(n, ckpt) and of adjoint_backward (the faster of two
+    calls) on fresh domains, for n = steps and n = steps // 2; and (J, gradients) of the full run.
+    The difference of the two lengths is the cost per step without the costs of a call (allocations,
+    the gradient download and its scaling on the host), which plain steps timed by CUDA events do
+    not carry either."""
+    import torch
+    from lbm_gb300 import build_domain
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = fn()
+        torch.cuda.synchronize()
+        return time.perf_counter() - t0, r
+
+    out, first = {}, None
+    for n in (steps, steps // 2):
+        with build_domain(scn, prec) as d:
+            d.step(0)
+            d.sync()
+            fwd, _ = timed(lambda: (d.adjoint_forward(n, ckpt), d.sync()))
+            J = d.objective_ke(box)
+            bwd, grads = timed(lambda: d.adjoint_backward(box))
+            bwd2, _ = timed(lambda: d.adjoint_backward(box))
+        out[n] = (fwd, min(bwd, bwd2))
+        if first is None:
+            first = (J, grads)
+    return {"steps": steps, "half": steps // 2, "t": out}, first
+
+
+def _adjoint_report(cost, plain_step):
+    n, h = cost["steps"], cost["half"]
+    (fwd, bwd), (fwd_h, bwd_h) = cost["t"][n], cost["t"][h]
+    fwd_step = (fwd - fwd_h) / (n - h)
+    bwd_step = (bwd - bwd_h) / (n - h)
+    return {
+        "forward_ckpt_ms_per_step": fwd_step * 1e3,
+        "backward_ms_per_step": bwd_step * 1e3,
+        "backward_over_forward": bwd_step / plain_step,
+        "forward_plus_backward_over_forward": (fwd_step + bwd_step) / plain_step,
+        "backward_call_ms": bwd * 1e3,
+        "backward_call_over_forward": bwd / (n * plain_step),
+        "backward_fixed_ms_per_call": (bwd - bwd_step * n) * 1e3,
+        "timing": f"wall clock around synchronised calls; per step = difference of {n}- and {h}-step "
+                  f"runs over {n - h} steps (a call's allocations, gradient download and host-side "
+                  f"scaling cancel); backward_call_* = the whole {n}-step call; plain steps by CUDA events",
     }
 
 
@@ -408,7 +437,6 @@ def run_cavity_adjoint(n=256, q=27, omega=1.8, lid=0.1, steps=500, ckpt=50, n_fd
     velocity, FP16 storage (FP32 adjoint arithmetic), checkpoints every `ckpt` steps, timed
     against plain FP16 steps on n^3. omega 1.8: at 1.95 the forward run itself diverges. dJ/du_x is
     checked on an n_fd^3 cavity against FP64 central differences (h = 1e-6)."""
-    import torch
     from lbm_gb300 import build_domain
     from lbm_gb300 import scenario as S
 
@@ -417,15 +445,7 @@ def run_cavity_adjoint(n=256, q=27, omega=1.8, lid=0.1, steps=500, ckpt=50, n_fd
     box = (1, n, 1, n, 1, n)
     with build_domain(make(n, lid), "fp16") as d:
         plain = time_steps(d, steps, 0)
-    with build_domain(make(n, lid), "fp16") as d:
-        d.step(0)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        d.adjoint_forward(steps, ckpt)
-        d.sync()
-        t1 = time.perf_counter()
-        _, gw = d.adjoint_backward(box)
-        t2 = time.perf_counter()
+    cost, (_, (_, gw)) = _adjoint_costs(make(n, lid), "fp16", steps, ckpt, box)
     fbox = (1, n_fd, 1, n_fd, 1, n_fd)
     with build_domain(make(n_fd, lid), "fp16") as d:
         d.adjoint_forward(steps, ckpt)
@@ -441,9 +461,7 @@ def run_cavity_adjoint(n=256, q=27, omega=1.8, lid=0.1, steps=500, ckpt=50, n_fd
                         f"checkpoint every {ckpt}, J = KE of the whole cavity",
             "storage": "fp16 (f - w), adjoint in fp32",
             "forward_plain_ms_per_step": plain / steps * 1e3,
-            "forward_ckpt_ms_per_step": (t1 - t0) / steps * 1e3,
-            "backward_ms_per_step": (t2 - t1) / steps * 1e3,
-            "backward_over_forward": (t2 - t1) / plain,
+            **_adjoint_report(cost, plain / steps),
             "dJ_du_lid": [float(x) for x in gw[1]],
             "fd_check": {"cells": n_fd ** 3, "fd_fp64_dJ_du_x": fd, "adjoint_fp16_dJ_du_x": float(gw_fd[1][0]),
                          "rel_err": abs(gw_fd[1][0] - fd) / abs(fd)}}

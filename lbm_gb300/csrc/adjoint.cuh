@@ -32,7 +32,7 @@ struct AdjParams {
     T omega;
     const T* mu_in;       // mu_t, Q planes of PS
     T* mu_out;            // mu_{t-1}
-    const T* rec;         // mass and momentum of g_{t-1}, 4 per cell (layout index)
+    const T* rec;         // mass and momentum of g_{t-1}, 4 per cell (layout index), 16-byte aligned
     int bc_terms;         // 1: the handler terms of step t apply (t >= s0 + 2)
     int write_mu;         // 0: only the theta gradients of step t
     double* grad_inflow;  // 3 per cell, reference cell order (inflow cells)
@@ -50,8 +50,22 @@ struct AdjConst<double> {
     static constexpr double A = 1.0 / kCS2, B = 1.0 / kCS4x2, C = 1.0 / kCS2x2;
 };
 
+// acc += s * v for a lattice component s in {-1, 0, 1} (a constant once the loops are unrolled).
+template <class T>
+__device__ __forceinline__ void add_signed(T& acc, T v, int s)
+{
+    if (s > 0) acc += v;
+    else if (s < 0) acc -= v;
+}
+
 // In place: lam <- J^T lam for the BGK map at a state of mass rho and momentum j:
-//   J = (1 - omega) I + omega d feq / dg,  feq_q = w_q rho (1 + A cu + B cu^2 - C uu)
+//   J = (1 - omega) I + omega d feq / dg,  feq_q = w_q rho (1 + A cu + B cu^2 - C uu).
+// (J^T lam)_p = (1 - omega) lam_p + omega (s0 + (c_p - u) . V) with
+//   s0 = sum_q w_q lam_q (1 + A cu_q + B cu_q^2 - C uu),
+//   V  = sum_q w_q lam_q ((A + 2 B cu_q) c_q - 2 C u),
+// and both depend on lam only through its ten weighted moments a = sum w lam, b = sum w lam c and
+// M = sum w lam c c^T: s0 = a (1 - C uu) + A u.b + B u.M u, V = A b + 2 B M u - 2 C a u. So the
+// per-direction work is signed adds (c has components -1, 0, 1) and one multiply-add.
 template <class L, class T>
 __device__ __forceinline__ void bgk_adjoint(T (&lam)[L::Q], T rho, T jx, T jy, T jz, T omega)
 {
@@ -59,25 +73,41 @@ __device__ __forceinline__ void bgk_adjoint(T (&lam)[L::Q], T rho, T jx, T jy, T
     const T ir = T(1) / rho;
     const T ux = jx * ir, uy = jy * ir, uz = jz * ir;
     const T uu = ux * ux + uy * uy + uz * uz;
-    T s0 = 0, vx = 0, vy = 0, vz = 0;
+    T a = 0, bx = 0, by = 0, bz = 0, mxx = 0, myy = 0, mzz = 0, mxy = 0, mxz = 0, myz = 0;
 #pragma unroll
     for (int q = 0; q < L::Q; ++q) {
-        const T cx = T(L::c(q, 0)), cy = T(L::c(q, 1)), cz = T(L::c(q, 2));
-        const T cu = cx * ux + cy * uy + cz * uz;
-        const T w = T(L::w(q));
-        const T lw = lam[q] * w;
-        s0 += lw * (T(1) + K::A * cu + K::B * cu * cu - K::C * uu);
-        const T g = lw * rho;
-        const T k1 = K::A + T(2) * K::B * cu;
-        vx += g * (k1 * cx - T(2) * K::C * ux);
-        vy += g * (k1 * cy - T(2) * K::C * uy);
-        vz += g * (k1 * cz - T(2) * K::C * uz);
+        const int cx = L::c(q, 0), cy = L::c(q, 1), cz = L::c(q, 2);
+        const T lw = lam[q] * T(L::w(q));
+        a += lw;
+        add_signed(bx, lw, cx);
+        add_signed(by, lw, cy);
+        add_signed(bz, lw, cz);
+        add_signed(mxx, lw, cx * cx);
+        add_signed(myy, lw, cy * cy);
+        add_signed(mzz, lw, cz * cz);
+        add_signed(mxy, lw, cx * cy);
+        add_signed(mxz, lw, cx * cz);
+        add_signed(myz, lw, cy * cz);
     }
+    const T mux = mxx * ux + mxy * uy + mxz * uz;
+    const T muy = mxy * ux + myy * uy + myz * uz;
+    const T muz = mxz * ux + myz * uy + mzz * uz;
+    const T s0 = a * (T(1) - K::C * uu) + K::A * (ux * bx + uy * by + uz * bz) +
+                 K::B * (ux * mux + uy * muy + uz * muz);
+    const T c2a = T(2) * K::C * a;
+    const T vx = K::A * bx + T(2) * K::B * mux - c2a * ux;
+    const T vy = K::A * by + T(2) * K::B * muy - c2a * uy;
+    const T vz = K::A * bz + T(2) * K::B * muz - c2a * uz;
+    const T k0 = omega * (s0 - (ux * vx + uy * vy + uz * vz));
+    const T wx = omega * vx, wy = omega * vy, wz = omega * vz;
     const T om1 = T(1) - omega;
 #pragma unroll
     for (int p = 0; p < L::Q; ++p) {
-        const T dx = T(L::c(p, 0)) - ux, dy = T(L::c(p, 1)) - uy, dz = T(L::c(p, 2)) - uz;
-        lam[p] = om1 * lam[p] + omega * (s0 + (dx * vx + dy * vy + dz * vz) * ir);
+        T t = k0;
+        add_signed(t, wx, L::c(p, 0));
+        add_signed(t, wy, L::c(p, 1));
+        add_signed(t, wz, L::c(p, 2));
+        lam[p] = om1 * lam[p] + t;
     }
 }
 
@@ -116,11 +146,20 @@ __device__ __forceinline__ void warp_flush_wall(double* grad_wall, int hid, cons
     }
 }
 
+// Blocks per SM the FP32 adjoint step is compiled for (0: no bound, FP64 is never bounded). 8 caps
+// it at 64 registers; D3Q27 then spills a few bytes in its handler path and the 256^3 cavity's
+// backward ran no faster (1.48 vs 1.47 ms per step), so the default leaves it unbounded.
+#ifndef LBMG_ADJ_MINB
+#define LBMG_ADJ_MINB 0
+#endif
+
 template <class L, class T>
-__global__ void __launch_bounds__(kBlockX) adjoint_step_kernel(const AdjParams<T> A)
+__global__ void __launch_bounds__(kBlockX, sizeof(T) == 4 ? LBMG_ADJ_MINB : 0) adjoint_step_kernel(const AdjParams<T> A)
 {
     using K = AdjConst<T>;
     constexpr int Q = L::Q;
+    grid_dep_wait();  // the previous adjoint step (or the kernel before it) has completed
+    grid_dep_launch();
     const int x = 1 + static_cast<int>(blockIdx.x) * kBlockX + static_cast<int>(threadIdx.x);
     const int y = 1 + static_cast<int>(blockIdx.y), z = 1 + static_cast<int>(blockIdx.z);
     const int i = cidx(A.g, x, y, z);
@@ -130,17 +169,26 @@ __global__ void __launch_bounds__(kBlockX) adjoint_step_kernel(const AdjParams<T
     double gw[3] = {0.0, 0.0, 0.0};
     if (active) {
         const size_t PS = A.g.PS;
+        const uint2 lw = fl != kFluidBulk ? A.link[i] : make_uint2(0u, kNoRecord);
+        const uint32_t link = lw.x;  // bit q: x - c_q is a boundary cell
+        // the links whose handler terms apply this step
+        const uint32_t own = A.bc_terms ? link : 0u;
         T lam[Q];
         // transposed pull: x's f*_p became the pulled g_p of x + c_p. Non-fluid cells hold 0 in
-        // every adjoint array (cleared once, never written), so no neighbour test is needed; bulk
-        // cells have no wrapped neighbour either.
+        // every adjoint array (cleared once, never written), so no neighbour test is needed. For a
+        // link q the pull of direction inv(q) meets such a cell; that slot reads x's own mu_q
+        // instead, the quantity every handler term of q starts from (for no-slip, lam[inv q] += mu_q
+        // is the whole term). Bulk cells have no wrapped neighbour either.
         if (fl != kFluidEdge) {  // no wrapped neighbour
             // one running pointer over the planes (block-uniform deltas), as the step's stores
             const int sy = A.g.XS, sz = A.g.XS * A.g.YS;
             const T* ptr = A.mu_in + i + (L::c(0, 0) + L::c(0, 1) * sy + L::c(0, 2) * sz);
 #pragma unroll
             for (int p = 0; p < Q; ++p) {
-                lam[p] = __ldcs(ptr);
+                const int qo = Q - 1 - p;  // the link whose pull partner is direction p
+                const long long self = static_cast<long long>(qo - p) * static_cast<long long>(PS) -
+                                       (L::c(p, 0) + L::c(p, 1) * sy + L::c(p, 2) * sz);
+                lam[p] = __ldcs(((own >> qo) & 1u) ? ptr + self : ptr);
                 if (p + 1 < Q) {
                     const int d = (L::c(p + 1, 0) - L::c(p, 0)) + (L::c(p + 1, 1) - L::c(p, 1)) * sy +
                                   (L::c(p + 1, 2) - L::c(p, 2)) * sz;
@@ -150,47 +198,47 @@ __global__ void __launch_bounds__(kBlockX) adjoint_step_kernel(const AdjParams<T
         } else {
 #pragma unroll
             for (int p = 0; p < Q; ++p) {
-                int mx, my, mz;
-                nbr_xyz(A.g, x, y, z, L::c(p, 0), L::c(p, 1), L::c(p, 2), mx, my, mz);
-                lam[p] = __ldcs(&A.mu_in[static_cast<size_t>(p) * PS + cidx(A.g, mx, my, mz)]);
+                const int qo = Q - 1 - p;
+                size_t k;
+                if ((own >> qo) & 1u) {
+                    k = static_cast<size_t>(qo) * PS + i;
+                } else {
+                    int mx, my, mz;
+                    nbr_xyz(A.g, x, y, z, L::c(p, 0), L::c(p, 1), L::c(p, 2), mx, my, mz);
+                    k = static_cast<size_t>(p) * PS + cidx(A.g, mx, my, mz);
+                }
+                lam[p] = __ldcs(&A.mu_in[k]);
             }
         }
-        const T rho_s = __ldcs(&A.rec[4 * static_cast<size_t>(i) + 0]);
-        const T jxs = __ldcs(&A.rec[4 * static_cast<size_t>(i) + 1]);
-        const T jys = __ldcs(&A.rec[4 * static_cast<size_t>(i) + 2]);
-        const T jzs = __ldcs(&A.rec[4 * static_cast<size_t>(i) + 3]);
-        const uint2 lw = fl != kFluidBulk ? A.link[i] : make_uint2(0u, kNoRecord);
-        const uint32_t link = lw.x;
+        T rho_s, jxs, jys, jzs;
+        ld_rec4(A.rec + 4 * static_cast<size_t>(i), rho_s, jxs, jys, jzs);
         // links whose handler needs its table entry: every link of a kFluidEdge cell; of a
-        // kFluidWall cell only those its LinkRecord lists (the others are no-slip)
-        uint32_t generic = link;
-        if (fl == kFluidWall) generic = (lw.y != kNoRecord && A.ltab) ? A.ltab[lw.y].spec : 0u;
-        if (A.bc_terms && link) {
+        // kFluidWall cell only those its LinkRecord lists (the others are no-slip, done above)
+        uint32_t generic = own;
+        if (fl == kFluidWall) generic = (lw.y != kNoRecord && A.ltab) ? A.ltab[lw.y].spec & own : 0u;
+        if (generic) {
             T spread = 0;              // added to every direction (handlers that use sum f*)
             T sx = 0, sy = 0, sz = 0;  // outflow / pressure: added as c_p . s
 #pragma unroll
             for (int q = 0; q < Q; ++q) {
-                if (!((link >> q) & 1u)) continue;
-                const T mu_q = A.mu_in[static_cast<size_t>(q) * PS + i];
+                if (!((generic >> q) & 1u)) continue;
                 const int qb = L::Q - 1 - q;
-                if (!((generic >> q) & 1u)) {  // no-slip: B_q = f*_qb
-                    lam[qb] += mu_q;
-                    continue;
-                }
+                const T mu_q = lam[qb];  // read by the pull above; the pull term itself is 0
                 int bx, by, bz;
                 nbr_xyz(A.g, x, y, z, -L::c(q, 0), -L::c(q, 1), -L::c(q, 2), bx, by, bz);
                 const uint8_t flb = A.flag[cidx(A.g, bx, by, bz)];
-                if (flb < kFirstHandler) continue;
+                if (flb < kFirstHandler) {  // no handler: no term
+                    lam[qb] = T(0);
+                    continue;
+                }
                 const int h = flb - kFirstHandler;
                 const BcEntry& be = A.bc[h];
                 switch (be.type) {
-                case kNoSlip:  // B_q = f*_qb
-                    lam[qb] += mu_q;
+                case kNoSlip:  // B_q = f*_qb: lam[qb] += mu_q, already in place
                     break;
                 case kMovingWall: {  // B_q = f*_qb + 2 w_q rho* (c_q . u_w) / cs2
                     const T cuw = T(L::c(q, 0)) * T(be.v[0]) + T(L::c(q, 1)) * T(be.v[1]) +
                                   T(L::c(q, 2)) * T(be.v[2]);
-                    lam[qb] += mu_q;
                     spread += mu_q * T(2) * T(L::w(q)) * cuw * K::A;
                     const double gcoef = static_cast<double>(mu_q * T(2) * T(L::w(q)) * rho_s * K::A);
                     if (wall_h < 0) wall_h = h;
@@ -205,7 +253,8 @@ __global__ void __launch_bounds__(kBlockX) adjoint_step_kernel(const AdjParams<T
                     }
                     break;
                 }
-                case kInflow: {  // B_q = feq_q(rho0, u_in)
+                case kInflow: {  // B_q = feq_q(rho0, u_in): no f* term
+                    lam[qb] = T(0);
                     const size_t r = ref_idx(A.g, bx, by, bz);
                     const double* v = be.has_profile ? A.profile + 3 * r : be.v;
                     const T vx = T(v[0]), vy = T(v[1]), vz = T(v[2]);
@@ -227,13 +276,14 @@ __global__ void __launch_bounds__(kBlockX) adjoint_step_kernel(const AdjParams<T
                     const T dx = wr * (T(4) * K::B * cu * T(L::c(q, 0)) - T(4) * K::C * ux);
                     const T dy = wr * (T(4) * K::B * cu * T(L::c(q, 1)) - T(4) * K::C * uy);
                     const T dz = wr * (T(4) * K::B * cu * T(L::c(q, 2)) - T(4) * K::C * uz);
-                    lam[qb] -= mu_q;
+                    lam[qb] = -mu_q;
                     sx += mu_q * dx / r0;
                     sy += mu_q * dy / r0;
                     sz += mu_q * dz / r0;
                     break;
                 }
                 default:
+                    lam[qb] = T(0);
                     break;
                 }
             }
@@ -266,9 +316,8 @@ __global__ void __launch_bounds__(kBlockX)
     const int y = 1 + static_cast<int>(blockIdx.y), z = 1 + static_cast<int>(blockIdx.z);
     const int i = cidx(g, x, y, z);
     if (!is_fluid(flag[i])) return;
-    const T rho = rec[4 * static_cast<size_t>(i)];
-    const T jx = rec[4 * static_cast<size_t>(i) + 1], jy = rec[4 * static_cast<size_t>(i) + 2],
-            jz = rec[4 * static_cast<size_t>(i) + 3];
+    T rho, jx, jy, jz;
+    ld_rec4(rec + 4 * static_cast<size_t>(i), rho, jx, jy, jz);
     const bool in = x >= box.x0 && x <= box.x1 && y >= box.y0 && y <= box.y1 && z >= box.z0 && z <= box.z1;
     const T ux = jx / rho, uy = jy / rho, uz = jz / rho;
     const T half_uu = T(0.5) * (ux * ux + uy * uy + uz * uz);

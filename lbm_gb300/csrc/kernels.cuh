@@ -365,7 +365,8 @@ struct StepParams {
     double* mon;           // kMonBuckets x 4 FP64 accumulators of the step's mass and momentum,
                            // or nullptr
     typename Store<S>::C* rec;  // per cell (layout index i): rec[4i..4i+3] = mass and momentum of
-                                // the populations the cell pulled this step, or nullptr
+                                // the populations the cell pulled this step, or nullptr; 16-byte
+                                // aligned (one vector store per cell)
     Geom g;
     double tau;
     float omega;
@@ -384,15 +385,35 @@ __device__ __forceinline__ void collide_any(typename Store<S>::C (&f)[L::Q], con
         collide_exact<L>(f, P.tau, m);
 }
 
+// The four record values of one cell, as whole vectors (one 16-byte access for FP32, two for
+// FP64): four scalar accesses 16 bytes apart would each touch four times the sectors they use.
+__device__ __forceinline__ void st_rec4(float* r, float a, float b, float c, float d)
+{
+    __stcs(reinterpret_cast<float4*>(r), make_float4(a, b, c, d));
+}
+__device__ __forceinline__ void st_rec4(double* r, double a, double b, double c, double d)
+{
+    __stcs(reinterpret_cast<double2*>(r), make_double2(a, b));
+    __stcs(reinterpret_cast<double2*>(r) + 1, make_double2(c, d));
+}
+__device__ __forceinline__ void ld_rec4(const float* r, float& a, float& b, float& c, float& d)
+{
+    const float4 v = __ldcs(reinterpret_cast<const float4*>(r));
+    a = v.x, b = v.y, c = v.z, d = v.w;
+}
+__device__ __forceinline__ void ld_rec4(const double* r, double& a, double& b, double& c, double& d)
+{
+    const double2 u = __ldcs(reinterpret_cast<const double2*>(r));
+    const double2 v = __ldcs(reinterpret_cast<const double2*>(r) + 1);
+    a = u.x, b = u.y, c = v.x, d = v.y;
+}
+
 // Stores a cell's pre-collision mass and momentum for the adjoint's recompute segments.
 template <class S>
 __device__ __forceinline__ void record_moments(typename Store<S>::C* rec, int i, const typename Store<S>::C (&m)[4])
 {
     using T = typename Store<S>::C;
-    __stcs(&rec[4 * static_cast<size_t>(i) + 0], Store<S>::kShifted ? T(1) + m[0] : m[0]);
-    __stcs(&rec[4 * static_cast<size_t>(i) + 1], m[1]);
-    __stcs(&rec[4 * static_cast<size_t>(i) + 2], m[2]);
-    __stcs(&rec[4 * static_cast<size_t>(i) + 3], m[3]);
+    st_rec4(rec + 4 * static_cast<size_t>(i), Store<S>::kShifted ? T(1) + m[0] : m[0], m[1], m[2], m[3]);
 }
 
 // Adds the warp's totals of m (the moments collide_any returned; zeros for a thread without a
@@ -839,6 +860,10 @@ __global__ void __launch_bounds__(kRowCells, min_blocks<L, S, ODD>())
 {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ __align__(8) uint64_t bars[kSegs];
+    // before any global access: the previous step (or whatever kernel precedes this one) has
+    // completed; then the next step's blocks may take the SMs this grid's last blocks leave
+    grid_dep_wait();
+    grid_dep_launch();
     const int b = static_cast<int>(blockIdx.x);
     const int interleaved = n_edge_blocks * static_cast<int>(edge_stride.d);
     const int e = static_cast<int>(fast_div(static_cast<uint32_t>(b), edge_stride));

@@ -44,6 +44,30 @@ StepParams<S> step_params(const DomainDev& d)
     return p;
 }
 
+// Programmatic dependent launch of the kernels that run back to back in the time loop (the step
+// and the adjoint step): their blocks may become resident while the previous kernel in the stream
+// finishes and wait at their top (grid_dep_wait) for it to complete, which hides the launch gap
+// between consecutive steps. LBMG_PDL 0 launches them plainly (tuning builds).
+#ifndef LBMG_PDL
+#define LBMG_PDL 1
+#endif
+template <class... KArgs, class... Args>
+inline void launch_chained(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                           const Args&... args)
+{
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cfg.attrs = attr;
+    cfg.numAttrs = LBMG_PDL ? 1 : 0;
+    cudaLaunchKernelEx(&cfg, kernel, args...);  // a failure is left for cudaGetLastError
+}
+
 template <int Q, class S>
 struct Launch {
     using L = Lattice<Q>;
@@ -102,7 +126,7 @@ struct Launch {
         const bool instr = mon_out != nullptr || rec != nullptr;
         auto* k = (t & 1) ? (instr ? step_kernel<L, S, true, true> : step_kernel<L, S, true, false>)
                           : (instr ? step_kernel<L, S, false, true> : step_kernel<L, S, false, false>);
-        k<<<blocks, kRowCells, smem, s>>>(p, n_edge_blocks, fes, nseg, fx, fy);
+        launch_chained(k, dim3(blocks), dim3(kRowCells), smem, s, p, n_edge_blocks, fes, nseg, fx, fy);
         if (mon_out) monitor_final_kernel<<<1, 256, 0, s>>>(d.mon, mon_out);
         side_passes(d, t, s);
     }
@@ -171,7 +195,7 @@ struct Launch {
         a.write_mu = write_mu;
         a.grad_inflow = grad_inflow;
         a.grad_wall = grad_wall;
-        adjoint_step_kernel<L, T><<<cell_grid(d.g), kBlockX, 0, s>>>(a);
+        launch_chained(adjoint_step_kernel<L, T>, cell_grid(d.g), dim3(kBlockX), 0, s, a);
     }
 
     static void objective_ke(const DomainDev& d, long long k, Box box, double* partials, int nblocks,

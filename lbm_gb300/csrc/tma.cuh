@@ -90,4 +90,12 @@ __device__ __forceinline__ void cp_async16(void* smem_dst, const void* gmem_src)
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
+// Programmatic dependent launch (griddepcontrol). grid_dep_wait blocks until the kernel this grid
+// follows in its stream has completed and its writes are visible; it returns at once for a launch
+// without the programmatic attribute. grid_dep_launch lets the next kernel in the stream, if it was
+// launched with that attribute, start its blocks once every block of this grid has issued it or
+// exited; they then wait in their own grid_dep_wait.
+__device__ __forceinline__ void grid_dep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void grid_dep_launch() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 }  // namespace lbmg
