@@ -18,6 +18,7 @@
 #pragma once
 
 #include "kernels.cuh"
+#include "state_kernels.cuh"  // kReduceThreads
 
 namespace lbmg {
 
@@ -52,7 +53,7 @@ struct AdjConst<double> {
 
 // acc += s * v for a lattice component s in {-1, 0, 1} (a constant once the loops are unrolled).
 template <class T>
-__device__ __forceinline__ void add_signed(T& acc, T v, int s)
+__host__ __device__ __forceinline__ void add_signed(T& acc, T v, int s)
 {
     if (s > 0) acc += v;
     else if (s < 0) acc -= v;
@@ -67,7 +68,7 @@ __device__ __forceinline__ void add_signed(T& acc, T v, int s)
 // M = sum w lam c c^T: s0 = a (1 - C uu) + A u.b + B u.M u, V = A b + 2 B M u - 2 C a u. So the
 // per-direction work is signed adds (c has components -1, 0, 1) and one multiply-add.
 template <class L, class T>
-__device__ __forceinline__ void bgk_adjoint(T (&lam)[L::Q], T rho, T jx, T jy, T jz, T omega)
+__host__ __device__ __forceinline__ void bgk_adjoint(T (&lam)[L::Q], T rho, T jx, T jy, T jz, T omega)
 {
     using K = AdjConst<T>;
     const T ir = T(1) / rho;
