@@ -165,7 +165,10 @@ int lbm_adjoint_objective_ke(lbm_domain* d, const int64_t box[6], double* J);
  * gradient with respect to the inflow velocity of each inflow cell (the per-cell profile or the
  * handler's uniform velocity at that cell); grad_wall (may be NULL): 3 doubles per handler id
  * (1-based id h at index 3*(h-1)), the gradient with respect to each moving wall's velocity. The
- * state is left as lbm_adjoint_forward left it. */
+ * state is left as lbm_adjoint_forward left it, so the call may be repeated (another box or dJ).
+ * Device memory for the call, freed before it returns: two adjoint population stores (Q values per
+ * cell in the compute type: FP32, or FP64 for FP64 storage), ckpt_every * 4 recorded values per
+ * cell, one copy of the population store and 3 doubles per cell. Synchronises. */
 int lbm_adjoint_backward(lbm_domain* d, const int64_t box[6], double dJ, double* grad_inflow,
                          double* grad_wall);
 

@@ -114,14 +114,15 @@ struct Launch {
         const FastDiv fx = make_fastdiv(static_cast<uint32_t>(nseg_x));
         const FastDiv fy = make_fastdiv(static_cast<uint32_t>(d.g.yl));
         constexpr size_t smem = row_smem_bytes<L, S>();
-        if constexpr (smem > 48 * 1024) {
-            static bool opted_in = false;
-            if (!opted_in) {
+        if constexpr (smem > 48 * 1024) {  // only with more than one segment per block
+            // once per process (a thread-safe static initialisation)
+            static const bool opted_in = [] {
                 for (auto k : {step_kernel<L, S, true, false>, step_kernel<L, S, false, false>,
                                step_kernel<L, S, true, true>, step_kernel<L, S, false, true>})
                     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-                opted_in = true;
-            }
+                return true;
+            }();
+            (void)opted_in;
         }
         const bool instr = mon_out != nullptr || rec != nullptr;
         auto* k = (t & 1) ? (instr ? step_kernel<L, S, true, true> : step_kernel<L, S, true, false>)
