@@ -418,20 +418,27 @@ __device__ __forceinline__ void record_moments(typename Store<S>::C* rec, int i,
 
 // Adds the warp's totals of m (the moments collide_any returned; zeros for a thread without a
 // cell, counted = false) to one accumulator bucket. Every lane of the warp must call it.
+// Shifted storage: m holds rho - 1 and j in FP32, values of order 1e-2, so the warp sums them in
+// FP32 (absolute error of order 1e-8 per warp) and lane 0 converts once; the 1 of every counted
+// cell enters as the exact cell count. An FP64 sum across the lanes costs about 25 FP64
+// operations per cell, as much time as the whole step at this GPU's FP64 rate. FP64 storage
+// keeps the FP64 warp sum. Buckets and the final sum are FP64 in both cases.
 template <class S>
 __device__ __forceinline__ void monitor_add(double* mon, const typename Store<S>::C (&m)[4], bool counted)
 {
-    double v[4] = {static_cast<double>(m[0]), static_cast<double>(m[1]), static_cast<double>(m[2]),
-                   static_cast<double>(m[3])};
-    if (Store<S>::kShifted && counted) v[0] += 1.0;
+    using T = typename Store<S>::C;
+    constexpr unsigned full = 0xffffffffu;
+    T v[4] = {m[0], m[1], m[2], m[3]};
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1)
 #pragma unroll
-        for (int k = 0; k < 4; ++k) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+        for (int k = 0; k < 4; ++k) v[k] += __shfl_down_sync(full, v[k], o);
+    const int n = Store<S>::kShifted ? __popc(__ballot_sync(full, counted)) : 0;
     if ((threadIdx.x & 31) == 0) {
         double* b = mon + 4 * ((blockIdx.x * 4 + (threadIdx.x >> 5)) % kMonBuckets);
+        atomicAdd(b + 0, static_cast<double>(v[0]) + static_cast<double>(n));
 #pragma unroll
-        for (int k = 0; k < 4; ++k) atomicAdd(b + k, v[k]);
+        for (int k = 1; k < 4; ++k) atomicAdd(b + k, static_cast<double>(v[k]));
     }
 }
 
