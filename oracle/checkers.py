@@ -12,18 +12,29 @@ ORACLE_DIR = Path(__file__).resolve().parent
 PORT_LIB = ORACLE_DIR / "liboracle.so"
 REF_LIB = ORACLE_DIR / "_ref" / "libref_lbm.so"
 REF_LIB_FAST = ORACLE_DIR / "_ref" / "libref_lbm_fast.so"
-REF_DIR = Path(os.environ.get("LBM_REFERENCE_DIR", "/root/reference"))
+
+
+def reference_dir() -> Path | None:
+    """The reference tree, named only by $LBM_REFERENCE_DIR (read at call time); None without it.
+    Only building oracle/_ref and regenerating the fixtures read the reference."""
+    d = os.environ.get("LBM_REFERENCE_DIR")
+    return Path(d) if d else None
+
 
 CONDITIONS = {"noslip": 1, "movingwall": 2, "freeslip": 3, "outflow": 4, "inflow": 5, "pressure": 6}
 
 
 def build(with_ref: bool | None = None) -> None:
-    """Compile the port (always) and the reference harness (when the reference tree exists)."""
+    """Compile the port (always) and the reference harness (when $LBM_REFERENCE_DIR names a
+    reference tree)."""
     subprocess.run(["make", "-s", "-C", str(ORACLE_DIR), "port"], check=True)
+    ref = reference_dir()
     if with_ref is None:
-        with_ref = (REF_DIR / "include" / "domain.hpp").exists()
+        with_ref = ref is not None and (ref / "include" / "domain.hpp").exists()
     if with_ref:
-        subprocess.run(["make", "-s", "-C", str(ORACLE_DIR), "ref", f"REF_DIR={REF_DIR}"], check=True)
+        if ref is None:
+            raise RuntimeError("LBM_REFERENCE_DIR is not set: the reference harness needs the reference tree")
+        subprocess.run(["make", "-s", "-C", str(ORACLE_DIR), "ref", f"REF_DIR={ref}"], check=True)
 
 
 def port_available() -> bool:

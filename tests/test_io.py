@@ -1,9 +1,12 @@
 """Scenario front end (config file, XML scenarios, legacy-VTK masks) and VTS output, on the CPU.
 
-The reference's own fixture files are read where the reference checkout is present; everything
-else uses files written here in the same formats.
+The reference's own scenario files are read from their committed copies under
+tests/golden/scenarios (the pipe mask gzip-compressed, checked against the SHA-256 of the
+reference's file); everything else uses files written here in the same formats.
 """
 import base64
+import gzip
+import hashlib
 import struct
 import xml.etree.ElementTree as ET
 from pathlib import Path
@@ -14,9 +17,21 @@ import pytest
 from lbm_gb300 import io
 from lbm_gb300 import scenario as S
 
-from oracle.checkers import REF_DIR
+REF_SCEN = Path(__file__).resolve().parent / "golden" / "scenarios"
 
-REF_SCEN = REF_DIR / "build" / "scenarios"
+
+def reference_scenarios(dest: Path) -> Path:
+    """The reference's build/scenarios files laid out as the reference runs them (from build/:
+    scenarios/<name>.xml, and scenarios/pipe.vtk, which pipe.xml names relative to the working
+    directory) under dest; returns dest. The pipe mask is checked against the reference's hash."""
+    sc = dest / "scenarios"
+    sc.mkdir(parents=True, exist_ok=True)
+    for name in ("cavity.xml", "pipe.xml", "shearflow.xml", "step.xml"):
+        (sc / name).write_bytes((REF_SCEN / name).read_bytes())
+    raw = gzip.decompress((REF_SCEN / "pipe.vtk.gz").read_bytes())
+    assert hashlib.sha256(raw).hexdigest() == (REF_SCEN / "pipe.vtk.sha256").read_text().strip()
+    (sc / "pipe.vtk").write_bytes(raw)
+    return dest
 
 STEP_XML = """<?xml version="1.0" ?>
 <scenario name="Backward step">
@@ -160,32 +175,40 @@ def test_vts_document_roundtrip():
 
 
 # ------------------------------------------------------------------------------------------
-# the reference's own scenario files, where the checkout is present
+# the reference's own scenario files (committed copies)
 # ------------------------------------------------------------------------------------------
-needs_ref = pytest.mark.skipif(not REF_SCEN.is_dir(), reason="reference checkout not present")
-
-
-@needs_ref
 @pytest.mark.parametrize("name", ["cavity.xml", "step.xml", "shearflow.xml", "pipe.xml"])
-def test_reference_scenario_files_parse(name):
-    scn = io.parse_scenario((REF_SCEN / name).read_text(), base_dir=REF_SCEN.parent)
+def test_reference_scenario_files_parse(name, tmp_path, monkeypatch):
+    base = reference_scenarios(tmp_path)
+    monkeypatch.chdir(base)
+    scn = io.parse_scenario((base / "scenarios" / name).read_text())
     assert scn.boundaries and scn.xl > 0
     if name == "pipe.xml":
+        assert scn.name == "Pipe flow"
         assert (scn.xl, scn.yl, scn.zl) == (250, 54, 54)
         assert scn.solid is not None and 0 < scn.solid.mean() < 1
+        assert [b.condition for b in scn.boundaries] == ["noslip", "noslip", "inflow", "outflow", "noslip",
+                                                         "noslip"]
+        assert scn.boundaries[2].v == (0.03, 0.0, 0.0)
 
 
-@needs_ref
-@pytest.mark.parametrize("name, steps", [("step.xml", 30), ("shearflow.xml", 30), ("cavity.xml", 10)])
-def test_reference_scenarios_port_equals_reference(name, steps, oracle_built):
-    # the parsed scenario run by the reference's own code and by the C port: bit for bit
+@pytest.mark.parametrize("name, steps", [("step.xml", 30), ("shearflow.xml", 30), ("cavity.xml", 10),
+                                         ("pipe.xml", 6)])
+def test_reference_scenarios_port_equals_reference(name, steps, oracle_built, tmp_path, monkeypatch):
+    # the parsed scenario run by the reference's own code and by the C port: bit for bit (the pipe
+    # mask marks its solid cells in one field only, as the reference's VTK reader does)
     import oracle
-    scn = io.parse_scenario((REF_SCEN / name).read_text(), q=19, tau=0.6)
+    if not oracle.ref_available():
+        pytest.skip("reference harness not built (needs the reference tree at build time)")
+    base = reference_scenarios(tmp_path)
+    monkeypatch.chdir(base)
+    scn = io.parse_scenario((base / "scenarios" / name).read_text(), q=19, tau=0.6)
+    mode = 1 if name == "pipe.xml" else 0
     try:
-        ref = oracle.run_ref(scn, steps)
+        ref = oracle.run_ref(scn, steps, solid_mode=mode, want_pops=False)
     except (OSError, RuntimeError) as e:
         pytest.skip(f"reference build unavailable: {e}")
-    port = oracle.run_port(scn, steps)
+    port = oracle.run_port(scn, steps, solid_mode=mode)
     assert np.array_equal(ref["rho"], port["rho"]) and np.array_equal(ref["u"], port["u"])
 
 
