@@ -1,5 +1,7 @@
 """bench.py on the host: the reference arm's JSON line at a small size carries the keys the bench
-contract names, and the adjoint cost arithmetic (difference of two run lengths) is right."""
+contract names (also when launched on two ranks), the adjoint cost arithmetic (difference of two
+run lengths) is right, and the replica aggregation of --gpus N (slowest rank's time, every rank's
+cells) holds on two gloo ranks."""
 import json
 import subprocess
 import sys
@@ -39,3 +41,56 @@ def test_adjoint_report_cancels_fixed_cost():
     assert rep["backward_over_forward"] == pytest.approx(per_b / plain)
     assert rep["backward_fixed_ms_per_call"] == pytest.approx(fixed_b * 1e3)
     assert rep["backward_call_over_forward"] == pytest.approx((fixed_b + per_b * 2000) / (2000 * plain))
+
+
+def _replica_worker(rank, world, port, q):
+    import os
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(world))
+    import torch.distributed as dist
+    sys.path.insert(0, str(ROOT))
+    import bench
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        sec = 0.5 + rank            # rank 1 is the slowest replica
+        bench.replica_barrier(world)
+        worst = bench.replica_max(sec, world)
+        q.put((rank, worst, bench.replica_mlups(1000, 10, worst, world)))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_replica_aggregation_two_ranks_gloo():
+    # bench.py --gpus N runs one independent domain per rank; the job's time is the slowest rank's
+    # and the value counts every rank's cells (world_size 2 over gloo on the host)
+    import multiprocessing as mp
+    import socket
+    with socket.socket() as sck:
+        sck.bind(("127.0.0.1", 0))
+        port = sck.getsockname()[1]
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    procs = [ctx.Process(target=_replica_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    out = sorted(q.get(timeout=120) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    assert [o[1] for o in out] == [1.5, 1.5]
+    assert all(o[2] == pytest.approx(2 * 1000 * 10 / 1.5 / 1e6) for o in out)
+
+
+def test_reference_arm_under_torchrun_two_ranks():
+    # the driver launches --impl reference like the GPU arm; rank 0 alone runs and prints
+    import socket
+    with socket.socket() as sck:
+        sck.bind(("127.0.0.1", 0))
+        port = sck.getsockname()[1]
+    r = subprocess.run([sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
+                        "--master-addr", "127.0.0.1", "--master-port", str(port), "bench.py", "--impl", "reference",
+                        "--size", "16,8,8", "--steps", "2", "--warmup", "1"],
+                       cwd=ROOT, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1
+    assert json.loads(lines[0])["impl"] == "reference"

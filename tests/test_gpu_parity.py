@@ -252,3 +252,67 @@ def test_step_monitor_counts_like_plain_steps():
         b.sync()
         assert a.steps_done == b.steps_done == 12
         assert np.array_equal(a.populations(), b.populations())
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp16"])
+@pytest.mark.parametrize("box", ["closed", "periodic"])
+def test_step_monitor_warp_sums_at_full_size(precision, box):
+    # The step monitor sums the shifted moments of a warp's 32 cells in FP32 and adds the warp's
+    # total to FP64 accumulators. On the 256 x 128 x 128 box that is 131,072 warps per step; the
+    # bound asserted is 1e-7 absolute per warp (each warp sum rounds five times, at most 2^-24
+    # of partial sums below 0.1). The comparison is exact in exact arithmetic: in a box closed by
+    # no-slip walls every post-collision population is pulled exactly once by the next step
+    # (bounce-back returns it to its own cell), so the mass the next step starts from is the mass
+    # lbm_reduce_mass_momentum finds; on a periodic box the momentum too.
+    xl, yl, zl = 256, 128, 128
+    scn = S.Scenario("Box", 19, xl, yl, zl, 1.0 / 1.8)
+    if box == "closed":
+        for f in ("z0", "zmax", "x0", "xmax", "y0", "ymax"):
+            scn.add_face(f, "noslip")
+        scn.solid = S.sphere_mask(xl, yl, zl, (64, 64, 64), 16)
+    else:
+        scn.periodic = (True, True, True)
+    rng = np.random.default_rng(11)
+    scn.init = np.tile(scn.model.weights, (scn.ncells, 1)) * (1 + 0.02 * rng.standard_normal((scn.ncells, 19)))
+    warps = ((xl + 127) // 128) * yl * zl * 4
+    bound = 1e-7 * warps
+    with build_domain(scn, precision) as dom:
+        dom.step(3)
+        for _ in range(2):
+            before = dom.reduce_mass_momentum()
+            tot = dom.step_monitored(1)
+            dom.sync()
+            err = np.abs(tot[0] - before)
+            print(f"{box} {precision}: mass error {err[0]:.3e}, momentum {err[1:].max():.3e} (bound {bound:.2e})")
+            assert err[0] <= bound
+            if box == "periodic":
+                assert err[1:].max() <= bound
+
+
+@pytest.mark.parametrize("steps_before", [0, 1])
+def test_chunked_transfers_roundtrip_and_continue(steps_before):
+    # 385 MB of FP64 D3Q27 populations: the upload and read-back go through the staging buffers
+    # in a dozen chunks (at most 32 MiB each), alternating between the two buffers; an arbitrary
+    # state set at either parity reads back unchanged and keeps stepping like the port started
+    # from the same state
+    scn = S.channel(200, 96, 88, q=27, sphere=((60, 48, 44), 12))
+    rng = np.random.default_rng(21)
+    f0 = np.tile(scn.model.weights, (scn.ncells, 1)) * (1 + 0.03 * rng.standard_normal((scn.ncells, 27)))
+    mask = defined_entries(scn)
+    with build_domain(scn, "fp64") as dom:
+        dom.step(steps_before)
+        dom.set_populations(f0)
+        back = dom.populations()
+        assert np.array_equal(back[mask], f0[mask])
+        dom.step(3)
+        got = dom.populations()
+        rho, u = dom.moments()
+    chk = oracle.Checker(scn)
+    chk.set_populations(f0)
+    chk.step(3)
+    want = chk.populations()
+    wr, wu = chk.moments()
+    chk.close()
+    assert np.array_equal(got[mask], want[mask])
+    fl = scn.fluid_mask_interior()
+    assert np.array_equal(rho[fl], wr[fl]) and np.array_equal(u[fl], wu[fl])
