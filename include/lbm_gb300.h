@@ -15,8 +15,11 @@
  *     x + (xl+2)*(y + (yl+2)*z) (domain.hpp:60-64); arrays over "interior cells" use
  *     (x-1) + xl*((y-1) + yl*(z-1)), the VTK writer's order (vtk.hpp:62-73).
  *   - Populations are exchanged as FP64 whatever the storage precision.
- *   - A handle owns its device memory and one CUDA stream; all work is ordered on that stream.
- *     lbm_step() is asynchronous; the read-back calls synchronise. One handle per host thread.
+ *   - A handle owns its device memory and one CUDA stream (plus a copy stream for the chunked
+ *     host transfers) on the device that was current at lbm_create; all work is ordered on that
+ *     stream. Every call makes the handle's device current while it runs and restores the
+ *     caller's current device before returning. lbm_step() is asynchronous; the read-back calls
+ *     synchronise. One handle per host thread.
  */
 #ifndef LBM_GB300_H
 #define LBM_GB300_H
@@ -95,13 +98,18 @@ int lbm_set_inflow_profile(lbm_domain* d, int handler, const double* u_cells);
 int lbm_set_nonfluid_cells_nullcollide(lbm_domain* d);
 
 /* Writes the current populations (the reference's collide_field, Domain::cell(x,y,z)[q],
- * domain.hpp:73-83) from a host array of Q doubles per cell over all cells. */
+ * domain.hpp:73-83) from a host array of Q doubles per cell over all cells. The array is moved
+ * in chunks through two staging buffers of the handle (at most 32 MiB each, allocated by the
+ * first transfer call and kept until lbm_destroy), each chunk's copy overlapping the previous
+ * chunk's conversion on the device; page-locked host memory makes the copies asynchronous.
+ * Synchronises. */
 int lbm_set_populations(lbm_domain* d, const double* f);
 
 /* Reads the current populations (collide_field) into a host array of Q doubles per cell over
  * all cells. Fluid cells hold their post-collision values; boundary cells hold what their
  * handler wrote in the last collide (boundary.hpp) in every direction that faces an interior
- * fluid cell, and the initial weight w_q in the other directions. */
+ * fluid cell, and the initial weight w_q in the other directions. Chunked through the staging
+ * buffers as lbm_set_populations. Synchronises. */
 int lbm_get_populations(lbm_domain* d, double* f);
 
 /* nsteps x { Domain::stream(); Domain::swap(); Domain::collide(); } -- domain.hpp:115-172,
@@ -111,10 +119,13 @@ int lbm_step(lbm_domain* d, int64_t nsteps);
 
 /* Extension: lbm_step with a conservation monitor. Each step also reduces, inside the step kernel,
  * the FP64 totals of the populations it pulled (the mass and momentum it started from: sum rho,
- * sum j_x, sum j_y, sum j_z over interior fluid cells) and copies them asynchronously to
- * totals[4*k .. 4*k+3] for the k-th step of the call. totals must hold 4*nsteps doubles and stay
- * valid until the next synchronising call; page-locked host memory keeps the copies
- * asynchronous. The totals are summed with atomics, so their last bits may differ between runs.
+ * sum j_x, sum j_y, sum j_z over interior fluid cells: each block adds its partial sums to FP64
+ * accumulators, which the next step's first block, or a one-block kernel after the call's last
+ * step, adds up) into a device ring of 1024 slots, which is copied asynchronously to
+ * totals[4*k .. 4*k+3] (the k-th step of the call) once per 1024 steps and after the last step.
+ * totals must hold 4*nsteps doubles and stay valid until the next synchronising call; page-locked
+ * host memory keeps the copies asynchronous. The totals are summed with atomics, so their last
+ * bits may differ between runs.
  * FP16 / BF16 / FP32 storage: each warp first sums its 32 cells' rho - 1 and j in FP32 (absolute
  * error of order 1e-8 per warp), and the warp sums are accumulated in FP64. FP64 storage sums in
  * FP64 throughout. */
@@ -122,17 +133,17 @@ int lbm_step_monitored(lbm_domain* d, int64_t nsteps, double* totals);
 
 /* Density and velocity of every interior cell (Cell::density / Cell::velocity on
  * collide_field, vtk.hpp:62-73), computed on the device in FP64. rho: one double per interior
- * cell; u: three (may be NULL). Synchronises. */
+ * cell; u: three (may be NULL). Chunked through the staging buffers as lbm_set_populations (the
+ * first transfer call of a handle allocates them). Synchronises. */
 int lbm_moments(lbm_domain* d, double* rho, double* u);
 
 /* No counterpart in the reference: lbm_moments for callers that must not allocate device memory.
- * Same results as lbm_moments (the same kernel), but the device buffer that holds the moments on
- * their way to the host is a static array inside the library (8 MiB, at most 262144 interior
- * cells; larger domains are rejected with LBM_ERR_ARG) instead of a cudaMalloc / cudaFree pair
- * per call. For callers whose device memory is owned by their own pool allocator (a cudaMalloc
- * would fail once the pool holds all free memory, or would make the pool give memory back), and
- * for loops that read the moments every step (the reference driver's timesteps-per-plot = 1),
- * where each cudaMalloc / cudaFree would synchronise the whole device.
+ * Same results as lbm_moments (the same arithmetic), but the device buffer that holds the moments
+ * on their way to the host is a static array inside the library (8 MiB, at most 262144 interior
+ * cells; larger domains are rejected with LBM_ERR_ARG) instead of the staging buffers that
+ * lbm_moments allocates on a handle's first transfer. For callers whose device memory is owned by
+ * their own pool allocator: a cudaMalloc would fail once the pool holds all free memory, or would
+ * make the pool give memory back, and a cudaMalloc / cudaFree pair synchronises the whole device.
  *   - The first call on a device looks up the array's device address (cudaGetSymbolAddress);
  *     make that first call before any stream capture.
  *   - All calls in the process share the array: calls whose work overlaps on the GPU (two handles
@@ -169,9 +180,11 @@ int lbm_adjoint_objective_ke(lbm_domain* d, const int64_t box[6], double* J);
  * handler's uniform velocity at that cell); grad_wall (may be NULL): 3 doubles per handler id
  * (1-based id h at index 3*(h-1)), the gradient with respect to each moving wall's velocity. The
  * state is left as lbm_adjoint_forward left it, so the call may be repeated (another box or dJ).
- * Device memory for the call, freed before it returns: two adjoint population stores (Q values per
- * cell in the compute type: FP32, or FP64 for FP64 storage), ckpt_every * 4 recorded values per
- * cell, one copy of the population store and 3 doubles per cell. Synchronises. */
+ * Device memory (allocated by the first call and kept with the handle for the next ones, until a
+ * geometry change, a run with another checkpoint interval, or lbm_destroy): two adjoint population
+ * stores (Q values per cell in the compute type: FP32, or FP64 for FP64 storage), ckpt_every * 4
+ * recorded values per cell, one copy of the population store and 3 doubles per cell. The
+ * gradients are scaled by dJ on the device and copied into the caller's arrays. Synchronises. */
 int lbm_adjoint_backward(lbm_domain* d, const int64_t box[6], double dJ, double* grad_inflow,
                          double* grad_wall);
 

@@ -27,8 +27,12 @@ using namespace lbmg;
 
 namespace {
 
-// Slots of the device ring that holds per-step monitor results until their copy to the host.
+// Slots of the device ring that holds per-step monitor results until their copy to the host (one
+// copy per kMonRing steps).
 constexpr int kMonRing = 1024;
+// Largest staging slot of the chunked host transfers (two slots per handle, allocated on the
+// first transfer and kept).
+constexpr size_t kStageSlotBytes = size_t(32) << 20;
 
 thread_local std::string g_create_error;
 
@@ -91,7 +95,14 @@ struct DevBuf {
     {
         release();
         if (count == 0) return;
-        check(cudaMalloc(reinterpret_cast<void**>(&p), count * sizeof(T)), what);
+        const cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&p), count * sizeof(T));
+        if (e != cudaSuccess) {
+            p = nullptr;
+            // a failed allocation is not a sticky error: clear it, so that a later
+            // cudaGetLastError of this thread does not report it against another call
+            cudaGetLastError();
+            check(e, what);
+        }
         n = count;
     }
     void release()
@@ -105,13 +116,23 @@ struct DevBuf {
 
 }  // namespace
 
-// Checkpoints of a gradient run (lbm_adjoint_forward .. lbm_adjoint_backward).
+// Checkpoints of a gradient run (lbm_adjoint_forward .. lbm_adjoint_backward), and the backward's
+// workspace: allocated by the first lbm_adjoint_backward of a run's geometry and checkpoint
+// interval and kept for the next calls, so that repeated gradients cost no allocation.
 struct AdjointRun {
     bool ready = false;
     long long s0 = 0;  // steps done when the run started
     long long n = 0;   // steps of the run
     long long k = 0;   // steps between checkpoints
     std::vector<std::unique_ptr<DevBuf<unsigned char>>> ckpt;  // state after s0 + j*k steps
+    DevBuf<unsigned char> mu[2];   // adjoint populations mu_t, mu_{t-1}
+    DevBuf<unsigned char> rec;     // the recorded mass and momentum of a segment's k steps
+    DevBuf<unsigned char> backup;  // the state the forward run left
+    DevBuf<double> gin, gwall;     // gradients (inflow cells, wall handlers)
+    void release_workspace()
+    {
+        mu[0].release(); mu[1].release(); rec.release(); backup.release(); gin.release(); gwall.release();
+    }
 };
 
 struct lbm_domain {
@@ -148,6 +169,17 @@ struct lbm_domain {
     DevBuf<int> errword;    // device error word, a list counter
     DevBuf<double> mon;     // step monitor accumulators
     DevBuf<double> mon_ring;  // per-step monitor results, kMonRing slots of 4 doubles
+    std::vector<int> gf_host;  // x, y, z of every ghost-fluid side-pass cell (as gf_xyz)
+
+    // Staging of the chunked host transfers (populations, moments): two device slots that take
+    // turns, so that the copy of one chunk (on copy_stream) overlaps the kernel of the other (on
+    // stream). Allocated by the first transfer and kept with the handle.
+    DevBuf<unsigned char> stage;
+    size_t stage_slot = 0;
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t ev_ready[2] = {nullptr, nullptr};  // slot filled (kernel done / upload done)
+    cudaEvent_t ev_free[2] = {nullptr, nullptr};   // slot consumed (download done / kernel done)
+    cudaEvent_t ev_start = nullptr;
 
     std::string err;
 
@@ -155,6 +187,13 @@ struct lbm_domain {
     {
         pop.release(); flag.release(); bc.release(); profile.release();
         gf_xyz.release(); gf_pop.release(); fs_link.release(); red.release(); link.release(); edge.release(); errword.release(); mon.release(); mon_ring.release();
+        stage.release();
+        for (int k = 0; k < 2; ++k) {
+            if (ev_ready[k]) cudaEventDestroy(ev_ready[k]);
+            if (ev_free[k]) cudaEventDestroy(ev_free[k]);
+        }
+        if (ev_start) cudaEventDestroy(ev_start);
+        if (copy_stream) cudaStreamDestroy(copy_stream);
         if (stream) cudaStreamDestroy(stream);
     }
 
@@ -195,9 +234,27 @@ struct lbm_domain {
     void build_edge_list();
     void build_link_table();
     void check_device_error();
+    void ensure_staging();
+    void upload_state(const double* f);
+    void download_state(double* f);
+    void download_moments(double* rho, double* u);
 };
 
 namespace {
+
+__global__ void scale_kernel(double* v, size_t n, double a)
+{
+    for (size_t k = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; k < n;
+         k += static_cast<size_t>(gridDim.x) * blockDim.x)
+        v[k] *= a;
+}
+
+void scale_doubles(double* v, size_t n, double a, cudaStream_t s)
+{
+    if (n == 0) return;
+    const size_t blocks = std::min<size_t>((n + 255) / 256, 4096);
+    scale_kernel<<<static_cast<unsigned>(blocks), 256, 0, s>>>(v, n, a);
+}
 
 // Appends the layout index of every kFluidEdge cell (the host sorts the list afterwards).
 __global__ void collect_edges_kernel(const uint8_t* flag, Geom g, int* list, int* count, int cap)
@@ -350,6 +407,7 @@ void lbm_domain::build_side_lists()
             }
 
     gf_xyz.release(); gf_pop.release(); fs_link.release();
+    gf_host = gxyz;
     dev.n_gf = static_cast<int>(gxyz.size() / 3);
     dev.n_fs = static_cast<int>(links.size());
     if (dev.n_gf > 0) {
@@ -378,6 +436,7 @@ void lbm_domain::finalize()
 {
     if (!geom_dirty) return;
     adj.ready = false;
+    adj.release_workspace();
     const Geom& g = dev.g;
     DevBuf<double> carry;
     if (state_custom) {
@@ -428,6 +487,124 @@ void lbm_domain::finalize()
     geom_dirty = false;
 }
 
+void lbm_domain::ensure_staging()
+{
+    if (stage.p) return;
+    const size_t need = std::max(ng * static_cast<size_t>(Q), 4 * n_interior) * sizeof(double);
+    stage_slot = std::min(kStageSlotBytes, (need + 255) / 256 * 256);
+    stage_slot = std::max(stage_slot, static_cast<size_t>(Q) * sizeof(double) * 256);
+    stage.alloc(2 * stage_slot, "cudaMalloc(transfer staging)");
+    check(cudaStreamCreateWithFlags(&copy_stream, cudaStreamNonBlocking), "cudaStreamCreate(copy)");
+    for (int k = 0; k < 2; ++k) {
+        check(cudaEventCreateWithFlags(&ev_ready[k], cudaEventDisableTiming), "cudaEventCreate");
+        check(cudaEventCreateWithFlags(&ev_free[k], cudaEventDisableTiming), "cudaEventCreate");
+    }
+    check(cudaEventCreateWithFlags(&ev_start, cudaEventDisableTiming), "cudaEventCreate");
+}
+
+// Host AoS FP64 field (reference cell order, all cells) -> state: chunk k is uploaded into slot
+// k % 2 on the copy stream while the scatter of chunk k - 1 runs on the handle's stream.
+void lbm_domain::upload_state(const double* f)
+{
+    ensure_staging();
+    const size_t row = static_cast<size_t>(Q) * sizeof(double);
+    const size_t rows = stage_slot / row;
+    check(cudaEventRecord(ev_start, stream), "cudaEventRecord");
+    check(cudaStreamWaitEvent(copy_stream, ev_start, 0), "cudaStreamWaitEvent");
+    size_t k = 0;
+    for (size_t r0 = 0; r0 < ng; r0 += rows, ++k) {
+        const size_t r1 = std::min(ng, r0 + rows);
+        const int slot = static_cast<int>(k & 1);
+        double* buf = reinterpret_cast<double*>(stage.p + slot * stage_slot);
+        if (k >= 2) check(cudaStreamWaitEvent(copy_stream, ev_free[slot], 0), "cudaStreamWaitEvent");
+        check(cudaMemcpyAsync(buf, f + r0 * Q, (r1 - r0) * row, cudaMemcpyHostToDevice, copy_stream),
+              "upload populations");
+        check(cudaEventRecord(ev_ready[slot], copy_stream), "cudaEventRecord");
+        check(cudaStreamWaitEvent(stream, ev_ready[slot], 0), "cudaStreamWaitEvent");
+        ops->scatter_range(dev, steps, r0, r1, buf, stream);
+        check(cudaEventRecord(ev_free[slot], stream), "cudaEventRecord");
+    }
+    check(cudaGetLastError(), "scatter kernel");
+    if (dev.n_gf > 0) {
+        // the ghost-fluid cells' side copy for this parity, then the slots they feed
+        std::vector<double> h(static_cast<size_t>(dev.n_gf) * Q);
+        for (int j = 0; j < dev.n_gf; ++j) {
+            const size_t r = ref_index(gf_host[3 * j], gf_host[3 * j + 1], gf_host[3 * j + 2]);
+            std::memcpy(h.data() + static_cast<size_t>(j) * Q, f + r * Q, row);
+        }
+        double* dst = gf_pop.p + static_cast<size_t>(steps & 1) * dev.n_gf * Q;
+        check(cudaMemcpyAsync(dst, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice, stream),
+              "upload ghost-fluid populations");
+        ops->ghost_fluid_slots(dev, steps, stream);
+        check(cudaGetLastError(), "ghost-fluid slots kernel");
+    }
+    check(cudaStreamSynchronize(stream), "set populations");
+}
+
+// State -> host AoS FP64 field: chunk k is gathered into slot k % 2 on the handle's stream while
+// the download of chunk k - 1 runs on the copy stream.
+void lbm_domain::download_state(double* f)
+{
+    ensure_staging();
+    const size_t row = static_cast<size_t>(Q) * sizeof(double);
+    const size_t rows = stage_slot / row;
+    size_t k = 0;
+    for (size_t r0 = 0; r0 < ng; r0 += rows, ++k) {
+        const size_t r1 = std::min(ng, r0 + rows);
+        const int slot = static_cast<int>(k & 1);
+        double* buf = reinterpret_cast<double*>(stage.p + slot * stage_slot);
+        if (k >= 2) check(cudaStreamWaitEvent(stream, ev_free[slot], 0), "cudaStreamWaitEvent");
+        ops->gather_range(dev, steps, r0, r1, buf, stream);
+        check(cudaEventRecord(ev_ready[slot], stream), "cudaEventRecord");
+        check(cudaStreamWaitEvent(copy_stream, ev_ready[slot], 0), "cudaStreamWaitEvent");
+        check(cudaMemcpyAsync(f + r0 * Q, buf, (r1 - r0) * row, cudaMemcpyDeviceToHost, copy_stream),
+              "download populations");
+        check(cudaEventRecord(ev_free[slot], copy_stream), "cudaEventRecord");
+    }
+    check(cudaGetLastError(), "gather kernel");
+    std::vector<double> h(static_cast<size_t>(dev.n_gf) * Q);
+    if (dev.n_gf > 0) {
+        const double* src = gf_pop.p + static_cast<size_t>(steps & 1) * dev.n_gf * Q;
+        check(cudaMemcpyAsync(h.data(), src, h.size() * sizeof(double), cudaMemcpyDeviceToHost, stream),
+              "download ghost-fluid populations");
+    }
+    check(cudaStreamSynchronize(copy_stream), "get populations");
+    check(cudaStreamSynchronize(stream), "get populations");
+    for (int j = 0; j < dev.n_gf; ++j) {
+        const size_t r = ref_index(gf_host[3 * j], gf_host[3 * j + 1], gf_host[3 * j + 2]);
+        std::memcpy(f + r * Q, h.data() + static_cast<size_t>(j) * Q, row);
+    }
+}
+
+// Interior density (and velocity) -> host, chunked as download_state.
+void lbm_domain::download_moments(double* rho, double* u)
+{
+    ensure_staging();
+    const size_t per = (u ? 4 : 1) * sizeof(double);
+    const size_t cells = stage_slot / per;
+    size_t k = 0;
+    for (size_t n0 = 0; n0 < n_interior; n0 += cells, ++k) {
+        const size_t n1 = std::min(n_interior, n0 + cells);
+        const int slot = static_cast<int>(k & 1);
+        double* buf = reinterpret_cast<double*>(stage.p + slot * stage_slot);
+        double* ubuf = u ? buf + (n1 - n0) : nullptr;
+        if (k >= 2) check(cudaStreamWaitEvent(stream, ev_free[slot], 0), "cudaStreamWaitEvent");
+        ops->moments_range(dev, steps, n0, n1, buf, ubuf, stream);
+        check(cudaEventRecord(ev_ready[slot], stream), "cudaEventRecord");
+        check(cudaStreamWaitEvent(copy_stream, ev_ready[slot], 0), "cudaStreamWaitEvent");
+        check(cudaMemcpyAsync(rho + n0, buf, (n1 - n0) * sizeof(double), cudaMemcpyDeviceToHost, copy_stream),
+              "download density");
+        if (u)
+            check(cudaMemcpyAsync(u + 3 * n0, ubuf, 3 * (n1 - n0) * sizeof(double), cudaMemcpyDeviceToHost,
+                                  copy_stream),
+                  "download velocity");
+        check(cudaEventRecord(ev_free[slot], copy_stream), "cudaEventRecord");
+    }
+    check(cudaGetLastError(), "moments kernel");
+    check(cudaStreamSynchronize(copy_stream), "moments");
+    check(cudaStreamSynchronize(stream), "moments");
+}
+
 namespace {
 
 // Device scratch of lbm_moments_noalloc: density and velocity of up to kNoAllocMaxCells interior
@@ -455,11 +632,29 @@ double* noalloc_scratch(int device)
     return g_noalloc_ptr[device];
 }
 
+// Makes the handle's device current for one call and restores the caller's device afterwards:
+// the handle's stream, memory and kernels belong to the device that was current at lbm_create.
+struct DeviceGuard {
+    int prev = -1;
+    int dev = -1;
+    explicit DeviceGuard(int device) : dev(device)
+    {
+        if (device < 0) return;
+        check(cudaGetDevice(&prev), "cudaGetDevice");
+        if (prev != device) check(cudaSetDevice(device), "cudaSetDevice");
+    }
+    ~DeviceGuard()
+    {
+        if (prev >= 0 && prev != dev) cudaSetDevice(prev);
+    }
+};
+
 template <class F>
 int guarded(lbm_domain* d, F&& f)
 {
     if (!d) return LBM_ERR_ARG;
     try {
+        DeviceGuard on_device(d->stream ? d->device : -1);  // lbm_create picks the device itself
         f();
         return LBM_OK;
     } catch (const CudaError& e) {
@@ -536,10 +731,10 @@ int lbm_create(lbm_domain** out, int q, int64_t xl, int64_t yl, int64_t zl, doub
         d->red.alloc(4 * kReduceBlocks + 4, "cudaMalloc(reduction scratch)");
         d->link.alloc(g.PS, "cudaMalloc(link words)");
         d->dev.link = d->link.p;
-        d->errword.alloc(2, "cudaMalloc(error word)");
+        d->errword.alloc(2, "cudaMalloc(error word)");  // error word, list counter
         check(cudaMemsetAsync(d->errword.p, 0, 2 * sizeof(int), d->stream), "clear error word");
         d->dev.err = d->errword.p;
-        d->mon.alloc(4 * kMonBuckets, "cudaMalloc(step monitor)");
+        d->mon.alloc(2 * 4 * kMonBuckets, "cudaMalloc(step monitor)");  // two accumulator sets
         check(cudaMemsetAsync(d->mon.p, 0, d->mon.bytes(), d->stream), "clear step monitor");
         d->dev.mon = d->mon.p;
         d->mon_ring.alloc(4 * kMonRing, "cudaMalloc(step monitor ring)");
@@ -567,8 +762,13 @@ int lbm_create(lbm_domain** out, int q, int64_t xl, int64_t yl, int64_t zl, doub
 void lbm_destroy(lbm_domain* d)
 {
     if (!d) return;
+    int prev = -1;
+    cudaGetDevice(&prev);
+    if (prev >= 0 && prev != d->device) cudaSetDevice(d->device);
+    const int dev = d->device;
     if (d->stream) cudaStreamSynchronize(d->stream);
-    delete d;
+    delete d;  // frees the handle's memory on its device
+    if (prev >= 0 && prev != dev) cudaSetDevice(prev);
 }
 
 int lbm_add_boundary(lbm_domain* d, int type, const double params[4], int* handler)
@@ -670,13 +870,8 @@ int lbm_set_populations(lbm_domain* d, const double* f)
     return guarded(d, [&] {
         if (!f) throw ArgError("f is NULL");
         d->finalize();
-        DevBuf<double> tmp;
-        tmp.alloc(d->ng * d->Q, "cudaMalloc(population staging)");
-        check(cudaMemcpyAsync(tmp.p, f, tmp.bytes(), cudaMemcpyHostToDevice, d->stream), "upload populations");
-        d->ops->scatter(d->dev, d->steps, tmp.p, d->stream);
-        check(cudaGetLastError(), "scatter kernel");
         d->adj.ready = false;
-        check(cudaStreamSynchronize(d->stream), "set populations");
+        d->upload_state(f);
         d->state_custom = true;
     });
 }
@@ -686,12 +881,7 @@ int lbm_get_populations(lbm_domain* d, double* f)
     return guarded(d, [&] {
         if (!f) throw ArgError("f is NULL");
         d->finalize();
-        DevBuf<double> tmp;
-        tmp.alloc(d->ng * d->Q, "cudaMalloc(population staging)");
-        d->ops->gather(d->dev, d->steps, tmp.p, d->stream);
-        check(cudaGetLastError(), "gather kernel");
-        check(cudaMemcpyAsync(f, tmp.p, tmp.bytes(), cudaMemcpyDeviceToHost, d->stream), "download populations");
-        check(cudaStreamSynchronize(d->stream), "get populations");
+        d->download_state(f);
         d->check_device_error();
     });
 }
@@ -701,7 +891,7 @@ int lbm_step(lbm_domain* d, int64_t nsteps)
     return guarded(d, [&] {
         if (nsteps < 0) throw ArgError("nsteps must be >= 0");
         d->finalize();
-        for (int64_t k = 0; k < nsteps; ++k) d->ops->step(d->dev, d->steps + 1 + k, nullptr, nullptr, d->stream);
+        for (int64_t k = 0; k < nsteps; ++k) d->ops->step(d->dev, d->steps + 1 + k, -1, nullptr, nullptr, d->stream);
         if (nsteps > 0) d->adj.ready = false;
         check(cudaGetLastError(), "step kernel launch");
         d->steps += nsteps;
@@ -715,11 +905,27 @@ int lbm_step_monitored(lbm_domain* d, int64_t nsteps, double* totals)
         if (nsteps < 0) throw ArgError("nsteps must be >= 0");
         if (!totals && nsteps > 0) throw ArgError("totals is NULL");
         d->finalize();
-        for (int64_t k = 0; k < nsteps; ++k) {
-            double* slot = d->mon_ring.p + 4 * (k % kMonRing);
-            d->ops->step(d->dev, d->steps + 1 + k, slot, nullptr, d->stream);
-            check(cudaMemcpyAsync(totals + 4 * k, slot, 4 * sizeof(double), cudaMemcpyDeviceToHost, d->stream),
+        // Step k adds into accumulator set k % 2; its totals land in ring slot k % kMonRing when the
+        // next step's first block (or, after the last step, the fold kernel) adds that set up. The
+        // ring goes to the host in whole groups of kMonRing slots, and the rest after the last fold.
+        auto slot = [&](int64_t k) { return d->mon_ring.p + 4 * (k % kMonRing); };
+        auto copy_out = [&](int64_t k0, int64_t n) {
+            check(cudaMemcpyAsync(totals + 4 * k0, slot(k0), static_cast<size_t>(n) * 4 * sizeof(double),
+                                  cudaMemcpyDeviceToHost, d->stream),
                   "copy step totals");
+        };
+        int64_t copied = 0;
+        for (int64_t k = 0; k < nsteps; ++k) {
+            d->ops->step(d->dev, d->steps + 1 + k, static_cast<int>(k & 1), k > 0 ? slot(k - 1) : nullptr, nullptr,
+                         d->stream);
+            if (k - copied == kMonRing) {  // slots copied .. k - 1 are written
+                copy_out(copied, kMonRing);
+                copied = k;
+            }
+        }
+        if (nsteps > 0) {
+            d->ops->monitor_fold(d->dev, static_cast<int>((nsteps - 1) & 1), slot(nsteps - 1), d->stream);
+            copy_out(copied, nsteps - copied);
         }
         check(cudaGetLastError(), "step kernel launch");
         d->steps += nsteps;
@@ -733,17 +939,7 @@ int lbm_moments(lbm_domain* d, double* rho, double* u)
     return guarded(d, [&] {
         if (!rho) throw ArgError("rho is NULL");
         d->finalize();
-        DevBuf<double> tmp;
-        tmp.alloc(d->n_interior * (u ? 4 : 1), "cudaMalloc(moments)");
-        d->ops->moments(d->dev, d->steps, tmp.p, u ? tmp.p + d->n_interior : nullptr, d->stream);
-        check(cudaGetLastError(), "moments kernel");
-        check(cudaMemcpyAsync(rho, tmp.p, d->n_interior * sizeof(double), cudaMemcpyDeviceToHost, d->stream),
-              "download density");
-        if (u)
-            check(cudaMemcpyAsync(u, tmp.p + d->n_interior, 3 * d->n_interior * sizeof(double),
-                                  cudaMemcpyDeviceToHost, d->stream),
-                  "download velocity");
-        check(cudaStreamSynchronize(d->stream), "moments");
+        d->download_moments(rho, u);
         d->check_device_error();
     });
 }
@@ -826,7 +1022,12 @@ int lbm_memory_info(const lbm_domain* d, uint64_t* device_bytes, uint64_t* step_
         m->finalize();
         if (device_bytes)
             *device_bytes = m->pop.bytes() + m->flag.bytes() + m->bc.bytes() + m->profile.bytes() + m->gf_xyz.bytes() +
-                            m->gf_pop.bytes() + m->fs_link.bytes() + m->red.bytes() + m->link.bytes() + m->edge.bytes() + m->errword.bytes() + m->mon.bytes() + m->mon_ring.bytes();
+                            m->gf_pop.bytes() + m->fs_link.bytes() + m->red.bytes() + m->link.bytes() + m->edge.bytes() +
+                            m->errword.bytes() + m->mon.bytes() + m->mon_ring.bytes() + m->stage.bytes() + m->ltab.bytes() +
+                            m->adj.mu[0].bytes() + m->adj.mu[1].bytes() + m->adj.rec.bytes() + m->adj.backup.bytes() +
+                            m->adj.gin.bytes() + m->adj.gwall.bytes();
+        if (device_bytes)
+            for (const auto& c : m->adj.ckpt) *device_bytes += c->bytes();
         if (step_bytes) *step_bytes = 2ull * m->Q * store_bytes(m->precision) * m->fluid_cells;
         if (fluid_cells) *fluid_cells = m->fluid_cells;
         if (launches_per_step)
@@ -871,7 +1072,7 @@ int lbm_adjoint_forward(lbm_domain* d, int64_t nsteps, int64_t ckpt_every)
             check(cudaMemcpyAsync(a.ckpt[j]->p, d->pop.p, d->pop.bytes(), cudaMemcpyDeviceToDevice, d->stream),
                   "store checkpoint");
             const long long len = std::min<long long>(ckpt_every, nsteps - j * ckpt_every);
-            for (long long r = 0; r < len; ++r) d->ops->step(d->dev, d->steps + 1 + r, nullptr, nullptr, d->stream);
+            for (long long r = 0; r < len; ++r) d->ops->step(d->dev, d->steps + 1 + r, -1, nullptr, nullptr, d->stream);
             d->steps += len;
         }
         check(cudaGetLastError(), "step kernel launch");
@@ -907,14 +1108,21 @@ int lbm_adjoint_backward(lbm_domain* d, const int64_t box[6], double dJ, double*
         const size_t PS = d->dev.g.PS;
         const size_t Tb = d->ops->compute_bytes;
         const size_t rec_bytes = 4 * PS * Tb;
-        DevBuf<unsigned char> mu[2], rec, backup;
-        DevBuf<double> gin, gwall;
-        mu[0].alloc(static_cast<size_t>(d->Q) * PS * Tb, "cudaMalloc(adjoint populations)");
-        mu[1].alloc(static_cast<size_t>(d->Q) * PS * Tb, "cudaMalloc(adjoint populations)");
-        rec.alloc(static_cast<size_t>(a.k) * rec_bytes, "cudaMalloc(recompute record)");
-        backup.alloc(d->pop.bytes(), "cudaMalloc(state backup)");
-        gin.alloc(3 * d->ng, "cudaMalloc(inflow gradient)");
-        gwall.alloc(3 * kMaxHandlers, "cudaMalloc(wall gradient)");
+        auto& mu = a.mu;
+        auto& rec = a.rec;
+        auto& backup = a.backup;
+        auto& gin = a.gin;
+        auto& gwall = a.gwall;
+        const size_t mu_bytes = static_cast<size_t>(d->Q) * PS * Tb;
+        if (mu[0].bytes() != mu_bytes || rec.bytes() != static_cast<size_t>(a.k) * rec_bytes) {
+            a.release_workspace();
+            mu[0].alloc(mu_bytes, "cudaMalloc(adjoint populations)");
+            mu[1].alloc(mu_bytes, "cudaMalloc(adjoint populations)");
+            rec.alloc(static_cast<size_t>(a.k) * rec_bytes, "cudaMalloc(recompute record)");
+            backup.alloc(d->pop.bytes(), "cudaMalloc(state backup)");
+            gin.alloc(3 * d->ng, "cudaMalloc(inflow gradient)");
+            gwall.alloc(3 * kMaxHandlers, "cudaMalloc(wall gradient)");
+        }
         check(cudaMemsetAsync(gin.p, 0, gin.bytes(), d->stream), "clear gradient");
         check(cudaMemsetAsync(gwall.p, 0, gwall.bytes(), d->stream), "clear gradient");
         check(cudaMemsetAsync(mu[0].p, 0, mu[0].bytes(), d->stream), "clear adjoint");
@@ -930,7 +1138,7 @@ int lbm_adjoint_backward(lbm_domain* d, const int64_t box[6], double dJ, double*
             check(cudaMemcpyAsync(d->pop.p, a.ckpt[j]->p, d->pop.bytes(), cudaMemcpyDeviceToDevice, d->stream),
                   "restore checkpoint");
             for (long long r = 1; r <= len; ++r)  // recompute, recording rec_{c+r}
-                d->ops->step(d->dev, c + r, nullptr, rec.p + (r - 1) * rec_bytes, d->stream);
+                d->ops->step(d->dev, c + r, -1, nullptr, rec.p + (r - 1) * rec_bytes, d->stream);
             if (j == nseg - 1) {
                 d->ops->adj_terminal(d->dev, rec.p + (len - 1) * rec_bytes, mu[cur].p, b, d->stream);
                 t_cur = c + len;
@@ -945,21 +1153,20 @@ int lbm_adjoint_backward(lbm_domain* d, const int64_t box[6], double dJ, double*
             }
         }
         check(cudaMemcpyAsync(d->pop.p, backup.p, d->pop.bytes(), cudaMemcpyDeviceToDevice, d->stream), "restore state");
+        // times the upstream gradient on the device, then straight into the caller's arrays
+        scale_doubles(gin.p, gin.n, dJ, d->stream);
+        scale_doubles(gwall.p, gwall.n, dJ, d->stream);
         check(cudaGetLastError(), "adjoint kernels");
         if (grad_inflow) {
             check(cudaMemcpyAsync(grad_inflow, gin.p, gin.bytes(), cudaMemcpyDeviceToHost, d->stream),
                   "download inflow gradient");
         }
-        std::vector<double> hw(3 * kMaxHandlers);
-        check(cudaMemcpyAsync(hw.data(), gwall.p, gwall.bytes(), cudaMemcpyDeviceToHost, d->stream),
-              "download wall gradient");
+        if (grad_wall && !d->bcs.empty())
+            check(cudaMemcpyAsync(grad_wall, gwall.p, 3 * d->bcs.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                                  d->stream),
+                  "download wall gradient");
         check(cudaStreamSynchronize(d->stream), "adjoint");
         d->check_device_error();
-        if (grad_inflow)
-            for (size_t k = 0; k < 3 * d->ng; ++k) grad_inflow[k] *= dJ;
-        if (grad_wall)
-            for (size_t h = 0; h < d->bcs.size(); ++h)
-                for (int k = 0; k < 3; ++k) grad_wall[3 * h + k] = dJ * hw[3 * h + k];
     });
 }
 

@@ -144,7 +144,8 @@ struct DomainDev {
     const LinkRecord* ltab;  // rows named by link[i].y
     // Device error word: set to 1 by a kernel whose bounded wait gave up.
     int* err;
-    // Step monitor accumulators (kMonBuckets x 4 doubles, zero between steps).
+    // Step monitor accumulators: two sets of kMonBuckets x 4 doubles, used by alternate monitored
+    // steps (each set is zero while unused).
     double* mon;
 };
 

@@ -156,7 +156,8 @@ __device__ __forceinline__ double momentum_exact(const double (&f)[L::Q], int d)
     return s;
 }
 
-// compute_feq (collision.hpp:33-51) for one direction q.
+// compute_feq (collision.hpp:33-51) for one direction q. Every division is the correctly
+// rounded division of divrn.cuh, bit-identical to the reference's.
 template <class L>
 __device__ __forceinline__ double feq_exact(int q, double rho, double u0, double u1, double u2)
 {
@@ -169,26 +170,66 @@ __device__ __forceinline__ double feq_exact(int q, double rho, double u0, double
     uu += u1 * u1;
     if (c2 > 0) cu += u2; else if (c2 < 0) cu -= u2;
     uu += u2 * u2;
-    return rt_w<L>(q) * rho * (1 + cu / kCS2 + (cu) * (cu) / kCS4x2 - uu / kCS2x2);
+    return rt_w<L>(q) * rho *
+           (1 + div_rn(cu, cs2_div()) + div_rn((cu) * (cu), cs4x2_div()) - div_rn(uu, cs2x2_div()));
 }
 
-// BGKCollision::collide (collision.hpp:60-70).
+// The three velocity components m[1..3] / rho (collision.hpp:27-29), correctly rounded: through
+// the reciprocal pair of rho where rho lies in div_rn's divisor range, by plain division otherwise
+// (a diverged state).
+__device__ __forceinline__ void velocity_exact(const double (&m)[4], double& u0, double& u1, double& u2)
+{
+    const double rho = m[0];
+    if (rho >= 0x1p-30 && rho <= 0x1p+30) {
+        const DivRN r = make_div_rn(rho, __drcp_rn(rho));
+        u0 = div_rn(m[1], r);
+        u1 = div_rn(m[2], r);
+        u2 = div_rn(m[3], r);
+    } else {
+        u0 = m[1] / rho;
+        u1 = m[2] / rho;
+        u2 = m[3] / rho;
+    }
+}
+
+// BGKCollision::collide (collision.hpp:60-70), operation for operation; tau is the relaxation
+// time's reciprocal pair. Opposite directions q and inv q = Q-1-q share their equilibrium terms:
+// c_{inv q}.u, summed in the reference's order, is exactly -(c_q.u) (or +0 where c_q.u is +0),
+// so cu/cs2 only changes sign (1 + a absorbs the sign of a zero) and cu^2/(2 cs4) is the same.
+// The equilibria are those of compute_feq bit for bit, with half the divisions.
 template <class L>
-__device__ __forceinline__ void collide_exact(double (&f)[L::Q], double tau, double (&m)[4])
+__device__ __forceinline__ void collide_exact(double (&f)[L::Q], const DivRN& tau, double (&m)[4])
 {
     const double rho = density_exact<L>(f);
     m[0] = rho;
     m[1] = momentum_exact<L>(f, 0);
     m[2] = momentum_exact<L>(f, 1);
     m[3] = momentum_exact<L>(f, 2);
-    const double u0 = m[1] / rho;
-    const double u1 = m[2] / rho;
-    const double u2 = m[3] / rho;
+    double u0, u1, u2;
+    velocity_exact(m, u0, u1, u2);
+    double uu = 0.0;
+    uu += u0 * u0;
+    uu += u1 * u1;
+    uu += u2 * u2;
+    const double c = div_rn(uu, cs2x2_div());
 #pragma unroll
-    for (int q = 0; q < L::Q; ++q) {
-        const double feq = feq_exact<L>(q, rho, u0, u1, u2);
-        f[q] -= (f[q] - feq) / tau;
+    for (int q = 0; q < L::REST; ++q) {
+        const int qb = L::Q - 1 - q;
+        double cu = 0.0;
+        if (L::c(q, 0) > 0) cu += u0; else if (L::c(q, 0) < 0) cu -= u0;
+        if (L::c(q, 1) > 0) cu += u1; else if (L::c(q, 1) < 0) cu -= u1;
+        if (L::c(q, 2) > 0) cu += u2; else if (L::c(q, 2) < 0) cu -= u2;
+        const double a = div_rn(cu, cs2_div());
+        const double b = div_rn((cu) * (cu), cs4x2_div());
+        const double wr = L::w(q) * rho;
+        const double feq = wr * (1 + a + b - c);
+        const double feqb = wr * (1 - a + b - c);
+        f[q] -= div_rn(f[q] - feq, tau);
+        f[qb] -= div_rn(f[qb] - feqb, tau);
     }
+    constexpr int R = L::REST;
+    const double feq = L::w(R) * rho * (1 + 0.0 + 0.0 - c);
+    f[R] -= div_rn(f[R] - feq, tau);
 }
 
 // Momentum sum_q f_q c_qd of populations kept in memory at fs[q * stride].
@@ -221,7 +262,7 @@ __device__ __forceinline__ double bc_value_exact(const BcEntry& b, int p, const 
         if (c1 > 0) cu += b.v[1]; else if (c1 < 0) cu -= b.v[1];
         if (c2 > 0) cu += b.v[2]; else if (c2 < 0) cu -= b.v[2];
         const double finv = fs[p * stride];
-        return finv + 2.0 * rt_w<L>(q) * rho_s * cu / kCS2;
+        return finv + div_rn(2.0 * rt_w<L>(q) * rho_s * cu, cs2_div());
     }
     case kInflow: {  // boundary.hpp:173-179
         const double* v = vcell ? vcell : b.v;
@@ -364,11 +405,13 @@ struct StepParams {
     int* err;              // set to 1 when a bounded wait gives up
     double* mon;           // kMonBuckets x 4 FP64 accumulators of the step's mass and momentum,
                            // or nullptr
+    double* mon_prev;      // the previous monitored step's accumulators, which block 0 adds up into
+    double* mon_prev_out;  // mon_prev_out[0..3] and clears; or nullptr
     typename Store<S>::C* rec;  // per cell (layout index i): rec[4i..4i+3] = mass and momentum of
                                 // the populations the cell pulled this step, or nullptr; 16-byte
                                 // aligned (one vector store per cell)
     Geom g;
-    double tau;
+    DivRN tau;             // relaxation time and its reciprocal pair (FP64 storage)
     float omega;
 };
 
@@ -414,32 +457,6 @@ __device__ __forceinline__ void record_moments(typename Store<S>::C* rec, int i,
 {
     using T = typename Store<S>::C;
     st_rec4(rec + 4 * static_cast<size_t>(i), Store<S>::kShifted ? T(1) + m[0] : m[0], m[1], m[2], m[3]);
-}
-
-// Adds the warp's totals of m (the moments collide_any returned; zeros for a thread without a
-// cell, counted = false) to one accumulator bucket. Every lane of the warp must call it.
-// Shifted storage: m holds rho - 1 and j in FP32, values of order 1e-2, so the warp sums them in
-// FP32 (absolute error of order 1e-8 per warp) and lane 0 converts once; the 1 of every counted
-// cell enters as the exact cell count. An FP64 sum across the lanes costs about 25 FP64
-// operations per cell, as much time as the whole step at this GPU's FP64 rate. FP64 storage
-// keeps the FP64 warp sum. Buckets and the final sum are FP64 in both cases.
-template <class S>
-__device__ __forceinline__ void monitor_add(double* mon, const typename Store<S>::C (&m)[4], bool counted)
-{
-    using T = typename Store<S>::C;
-    constexpr unsigned full = 0xffffffffu;
-    T v[4] = {m[0], m[1], m[2], m[3]};
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1)
-#pragma unroll
-        for (int k = 0; k < 4; ++k) v[k] += __shfl_down_sync(full, v[k], o);
-    const int n = Store<S>::kShifted ? __popc(__ballot_sync(full, counted)) : 0;
-    if ((threadIdx.x & 31) == 0) {
-        double* b = mon + 4 * ((blockIdx.x * 4 + (threadIdx.x >> 5)) % kMonBuckets);
-        atomicAdd(b + 0, static_cast<double>(v[0]) + static_cast<double>(n));
-#pragma unroll
-        for (int k = 1; k < 4; ++k) atomicAdd(b + k, static_cast<double>(v[k]));
-    }
 }
 
 // Handler values of an edge cell: for every direction p toward a non-fluid neighbour m (bit
@@ -537,7 +554,16 @@ __device__ __forceinline__ void store_edge_populations(const StepParams<S>& P, i
 #endif
 constexpr int kRowCells = LBMG_ROW_CELLS;
 constexpr int kSegs = LBMG_SEGS;
+constexpr int kMonFoldThreads = kRowCells;  // threads of a step-kernel block
 constexpr uint32_t kMaxPolls = 1u << 20;
+// Polls of a row block's first wait for its staged rows. The failure tests build a copy of the
+// library with 0 here, so that every such wait gives up at once and runs the give-up path (error
+// word, the drain wait with the full limit kMaxPolls, no update of the segment) without any wait
+// being left unbounded.
+#ifndef LBMG_ROW_WAIT_POLLS
+#define LBMG_ROW_WAIT_POLLS (1u << 20)
+#endif
+constexpr uint32_t kRowWaitPolls = LBMG_ROW_WAIT_POLLS;
 
 template <class S>
 constexpr int row_pad()
@@ -566,8 +592,72 @@ constexpr size_t row_smem_bytes()
     return kSegs * stage_bytes<L, S>() + link_smem_bytes<S>();
 }
 
+// Step monitor. Each block adds the moments its cells started from (m as collide_any returns them,
+// accumulated over the block's segments in macc; ncell cells counted) to one of kMonBuckets FP64
+// accumulators, one atomic per quantity and block. Shifted storage: m holds rho - 1 and j in FP32,
+// values of order 1e-2, so each warp sums them in FP32 (absolute error of order 1e-8 per warp) and
+// its lane 0 converts once; the 1 of every counted cell enters as the exact cell count. An FP64
+// sum across the lanes costs about 25 FP64 operations per cell, as much time as the whole step at
+// this GPU's FP64 rate. FP64 storage keeps FP64 sums. The four warps' sums are added in FP64, in
+// a fixed order. Every thread of the block must call it.
+template <class S>
+__device__ __forceinline__ void monitor_block_add(double* mon, const typename Store<S>::C (&macc)[4], int ncell)
+{
+    using T = typename Store<S>::C;
+    constexpr unsigned full = 0xffffffffu;
+    __shared__ double s_part[kMonFoldThreads / 32][4];
+    T v[4] = {macc[0], macc[1], macc[2], macc[3]};
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+        for (int k = 0; k < 4; ++k) v[k] += __shfl_down_sync(full, v[k], o);
+    const int n = Store<S>::kShifted ? __reduce_add_sync(full, ncell) : 0;
+    if ((threadIdx.x & 31) == 0) {
+        s_part[threadIdx.x >> 5][0] = static_cast<double>(v[0]) + static_cast<double>(n);
+#pragma unroll
+        for (int k = 1; k < 4; ++k) s_part[threadIdx.x >> 5][k] = static_cast<double>(v[k]);
+    }
+    __syncthreads();
+    if (threadIdx.x < 4) {
+        double t = 0.0;
+#pragma unroll
+        for (int w = 0; w < kMonFoldThreads / 32; ++w) t += s_part[w][threadIdx.x];
+        atomicAdd(mon + 4 * (blockIdx.x % kMonBuckets) + threadIdx.x, t);
+    }
+}
+
+// Sums kMonBuckets x 4 accumulators in a fixed order into out[0..3] and clears them; one block of
+// kMonFoldThreads threads. It runs in the first block of the next monitored step (after
+// grid_dep_wait, so every addition of the step it folds has completed) or, after the last step,
+// in monitor_fold_kernel.
+__device__ __forceinline__ void monitor_fold(double* mon, double* out)
+{
+    __shared__ double s_fold[kMonFoldThreads / 32][4];
+    double v[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int b = static_cast<int>(threadIdx.x); b < kMonBuckets; b += kMonFoldThreads)
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            v[k] += __ldcg(mon + 4 * b + k);
+            mon[4 * b + k] = 0.0;
+        }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+        if ((threadIdx.x & 31) == 0) s_fold[threadIdx.x >> 5][k] = v[k];
+    }
+    __syncthreads();
+    if (threadIdx.x < 4) {
+        double t = 0.0;
+#pragma unroll
+        for (int w = 0; w < kMonFoldThreads / 32; ++w) t += s_fold[w][threadIdx.x];
+        out[threadIdx.x] = t;
+    }
+}
+
 template <class L, class S, bool ODD, bool INSTR>
-__device__ __forceinline__ void edge_block(const StepParams<S>& P, int blk, unsigned char* smem_raw)
+__device__ __forceinline__ void edge_block(const StepParams<S>& P, int blk, unsigned char* smem_raw,
+                                           typename Store<S>::C (&macc)[4], int& ncell)
 {
     using St = Store<S>;
     using T = typename St::C;
@@ -604,7 +694,11 @@ __device__ __forceinline__ void edge_block(const StepParams<S>& P, int blk, unsi
             store_handler_values<L, S, ODD>(P, x, y, z, i, link, fs, kRowCells);
         }
     }
-    if (INSTR && P.mon) monitor_add<S>(P.mon, m, j < P.n_edge);
+    if constexpr (INSTR) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) macc[k] += m[k];
+        ncell += j < P.n_edge;
+    }
 }
 
 __device__ __forceinline__ void segment_origin(const Geom& g, int seg, const FastDiv& dx, const FastDiv& dy, int& x0,
@@ -719,7 +813,8 @@ __device__ __forceinline__ V opaque(V v)
 
 template <class L, class S, bool ODD, bool INSTR>
 __device__ __forceinline__ void row_block(const StepParams<S>& P, int rb, int nseg, const FastDiv& dx, const FastDiv& dy,
-                                          unsigned char* smem_raw, uint64_t* bars)
+                                          unsigned char* smem_raw, uint64_t* bars, typename Store<S>::C (&macc)[4],
+                                          int& ncell)
 {
     using St = Store<S>;
     using T = typename St::C;
@@ -788,8 +883,9 @@ __device__ __forceinline__ void row_block(const StepParams<S>& P, int rb, int ns
                 cp_async_commit();
             }
         }
-        if (!mbar_wait_bounded(&bars[s], 0, kMaxPolls)) {
-            // the step's results are invalid; still never leave while copies may land here
+        if (!mbar_wait_bounded(&bars[s], 0, kRowWaitPolls)) {
+            // the step's results are invalid; still never leave while copies may land here (this
+            // drain wait is bounded too: if it also gives up the block returns regardless)
             *P.err = 1;
             mbar_wait_bounded(&bars[s], 0, kMaxPolls);
             bulk = false;
@@ -818,24 +914,29 @@ __device__ __forceinline__ void row_block(const StepParams<S>& P, int rb, int ns
         } else if constexpr (St::kShifted) {
             if (rec) cp_async_wait_all();  // no copy may still be landing when the block ends
         }
-        if (INSTR && P.mon) monitor_add<S>(P.mon, m, bulk);
+        if constexpr (INSTR) {
+#pragma unroll
+            for (int k = 0; k < 4; ++k) macc[k] += m[k];
+            ncell += bulk;
+        }
     }
 }
 
 // Resident blocks per SM that the register allocation of a step kernel must allow (0: no
 // bound; ptxas then picks fewer registers than with an explicit 1). Unbounded, the shifted
-// D3Q19 kernels take 56 registers (9 blocks per SM); bounded to 10 blocks they keep 48, and so do
-// the D3Q15 ones (one odd-step spill of 4 bytes, 2% faster than 56 registers). D3Q27 gains
-// nothing from a bound; FP64 is never bounded. LBMG_MINB_Q15 / LBMG_MINB_Q27 set the D3Q15 and
+// D3Q19 kernels take 56 registers (9 blocks per SM); bounded to 10 blocks they keep 48. The
+// D3Q15 ones run at 12 blocks per SM (40 registers): 46.7k against 43.9k MLUPS at 10 blocks on
+// the 256x128x128 channel in FP32. D3Q27 gains nothing from a bound (6, 7 and 8 blocks: 20.9k,
+// 23.1k, 23.3k against 23.4k unbounded); FP64 is never bounded. LBMG_MINB_Q15 / LBMG_MINB_Q27 set the D3Q15 and
 // D3Q27 values in tuning builds. LBMG_MINB_EVEN / LBMG_MINB_ODD override the shifted-storage
 // values in tuning builds.
 #ifndef LBMG_MINB_Q15
-#define LBMG_MINB_Q15 10
+#define LBMG_MINB_Q15 12
 #endif
 #ifndef LBMG_MINB_Q27
 #define LBMG_MINB_Q27 0
 #endif
-template <class L, class S, bool ODD>
+template <class L, class S, bool ODD, bool INSTR>
 constexpr int min_blocks()
 {
     if constexpr (!Store<S>::kShifted) {
@@ -847,6 +948,8 @@ constexpr int min_blocks()
 #if defined(LBMG_MINB_EVEN)
         if (!ODD) return LBMG_MINB_EVEN;
 #endif
+        // the instrumented D3Q15 kernels (monitor, adjoint record) would spill at 40 registers
+        if (INSTR && L::Q == 15) return 10;
         return L::Q == 19 ? 10 : L::Q == 27 ? LBMG_MINB_Q27 : LBMG_MINB_Q15;
     }
 }
@@ -862,7 +965,7 @@ constexpr double kEdgeSpan = LBMG_EDGE_SPAN;
 // INSTR: the step monitor and the adjoint's record may be active (P.mon / P.rec are tested);
 // plain steps are compiled without them.
 template <class L, class S, bool ODD, bool INSTR>
-__global__ void __launch_bounds__(kRowCells, min_blocks<L, S, ODD>())
+__global__ void __launch_bounds__(kRowCells, min_blocks<L, S, ODD, INSTR>())
     step_kernel(const StepParams<S> P, int n_edge_blocks, FastDiv edge_stride, int nseg, FastDiv nseg_x, FastDiv yl)
 {
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -872,14 +975,29 @@ __global__ void __launch_bounds__(kRowCells, min_blocks<L, S, ODD>())
     grid_dep_wait();
     grid_dep_launch();
     const int b = static_cast<int>(blockIdx.x);
+    if constexpr (INSTR) {
+        if (P.mon_prev && b == 0) monitor_fold(P.mon_prev, P.mon_prev_out);
+    }
+    using T = typename Store<S>::C;
+    T macc[4] = {T(0), T(0), T(0), T(0)};
+    int ncell = 0;
     const int interleaved = n_edge_blocks * static_cast<int>(edge_stride.d);
     const int e = static_cast<int>(fast_div(static_cast<uint32_t>(b), edge_stride));
     if (b < interleaved && b == e * static_cast<int>(edge_stride.d))
-        edge_block<L, S, ODD, INSTR>(P, e, smem_raw);
+        edge_block<L, S, ODD, INSTR>(P, e, smem_raw, macc, ncell);
     else if (b < interleaved)
-        row_block<L, S, ODD, INSTR>(P, b - (e + 1), nseg, nseg_x, yl, smem_raw, bars);
+        row_block<L, S, ODD, INSTR>(P, b - (e + 1), nseg, nseg_x, yl, smem_raw, bars, macc, ncell);
     else
-        row_block<L, S, ODD, INSTR>(P, b - n_edge_blocks, nseg, nseg_x, yl, smem_raw, bars);
+        row_block<L, S, ODD, INSTR>(P, b - n_edge_blocks, nseg, nseg_x, yl, smem_raw, bars, macc, ncell);
+    if constexpr (INSTR) {
+        if (P.mon) monitor_block_add<S>(P.mon, macc, ncell);
+    }
+}
+
+// The fold of the last monitored step of a call (see monitor_fold).
+static __global__ void __launch_bounds__(kMonFoldThreads) monitor_fold_kernel(double* mon, double* out)
+{
+    monitor_fold(mon, out);
 }
 
 // ------------------------------------------------------------------------------------------

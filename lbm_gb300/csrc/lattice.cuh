@@ -8,6 +8,8 @@
 
 #include <cstdint>
 
+#include "divrn.cuh"
+
 namespace lbmg {
 
 // lbmdefinitions.h:47 defines C_S as 0.57735026919l converted to double; this hex literal is
@@ -17,6 +19,11 @@ constexpr double kCS = 0x1.279a745904047p-1;
 constexpr double kCS2 = kCS * kCS;                     // C_S * C_S          (collision.hpp:45)
 constexpr double kCS4x2 = 2 * kCS * kCS * kCS * kCS;   // 2*C_S*C_S*C_S*C_S  (collision.hpp:45)
 constexpr double kCS2x2 = 2 * kCS * kCS;               // 2*C_S*C_S          (collision.hpp:46)
+// The three divisors with their reciprocal pairs {y, RN(1/y), RN((1 - y RN(1/y)) / y)} for
+// div_rn (divrn.cuh); the host check tests/cpp/div_rn_check.cpp recomputes them.
+__host__ __device__ constexpr DivRN cs2_div() { return {kCS2, 0x1.7ffffffffddcap+1, 0x1.000000c30db6dp-53}; }
+__host__ __device__ constexpr DivRN cs4x2_div() { return {kCS4x2, 0x1.1ffffffffccb0p+2, -0x1.17fffdb6dee01p-52}; }
+__host__ __device__ constexpr DivRN cs2x2_div() { return {kCS2x2, 0x1.7ffffffffddcap+0, 0x1.000000c30db6dp-54}; }
 
 template <int QQ>
 struct Lattice;

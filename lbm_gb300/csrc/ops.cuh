@@ -14,16 +14,29 @@ struct KernelOps {
     void (*init)(const DomainDev& d, cudaStream_t s);
     // fluid cells -> kFluidBulk / kFluidEdge
     void (*classify)(const DomainDev& d, cudaStream_t s);
-    // one time step number `t` (1-based): fused kernel, then the side passes; with mon_out
-    // (device, 4 doubles) also the FP64 mass and momentum the step started from; with rec
-    // (device, 4 compute-type values per cell) each cell's pre-collision mass and momentum
-    void (*step)(const DomainDev& d, long long t, double* mon_out, void* rec, cudaStream_t s);
+    // one time step number `t` (1-based): fused kernel, then the side passes. Monitored steps
+    // (mon_set 0 or 1; -1: none) add the FP64 mass and momentum the step started from into that
+    // accumulator set, and with prev_out the step's first block first folds the other set (the
+    // previous monitored step's) into prev_out (device, 4 doubles). With rec (device, 4
+    // compute-type values per cell) each cell's pre-collision mass and momentum.
+    void (*step)(const DomainDev& d, long long t, int mon_set, double* prev_out, void* rec, cudaStream_t s);
+    // folds accumulator set mon_set into out (device, 4 doubles): the last monitored step of a call
+    void (*monitor_fold)(const DomainDev& d, int mon_set, double* out, cudaStream_t s);
     // state after `k` steps -> AoS FP64 over all cells (device buffer)
     void (*gather)(const DomainDev& d, long long k, double* out, cudaStream_t s);
     // AoS FP64 over all cells (device buffer) -> state after `k` steps
     void (*scatter)(const DomainDev& d, long long k, const double* in, cudaStream_t s);
     // interior moments (device buffers)
     void (*moments)(const DomainDev& d, long long k, double* rho, double* u, cudaStream_t s);
+    // chunked host transfers through staging buffers: rows [r0, r1) of the AoS FP64 field (reference
+    // cell order) out of / into the state after `k` steps (ghost-fluid cells excluded), and the
+    // moments of the interior cells [n0, n1) (interior order)
+    void (*gather_range)(const DomainDev& d, long long k, size_t r0, size_t r1, double* out, cudaStream_t s);
+    void (*scatter_range)(const DomainDev& d, long long k, size_t r0, size_t r1, const double* in, cudaStream_t s);
+    void (*moments_range)(const DomainDev& d, long long k, size_t n0, size_t n1, double* rho, double* u,
+                          cudaStream_t s);
+    // the boundary slots fed by the ghost-fluid cells, from their side copy for step parity k & 1
+    void (*ghost_fluid_slots)(const DomainDev& d, long long k, cudaStream_t s);
     // FP64 totals into out[4] (device), partials: scratch of 4 * reduce_blocks doubles
     void (*reduce)(const DomainDev& d, long long k, double* partials, int reduce_blocks,
                    double* out, cudaStream_t s);

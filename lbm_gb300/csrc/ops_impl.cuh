@@ -3,6 +3,7 @@
 #pragma once
 
 #include <algorithm>
+#include <mutex>
 
 #include "ops.cuh"
 #include "state_kernels.cuh"
@@ -17,11 +18,16 @@ inline dim3 cell_grid(const Geom& g)
                 static_cast<unsigned>(g.zl));
 }
 
+constexpr int kMaxDevices = 64;
+
 inline unsigned linear_blocks(size_t n, unsigned threads)
 {
     const size_t b = (n + threads - 1) / threads;
     return static_cast<unsigned>(b < 65535u * 16u ? (b > 0 ? b : 1) : 65535u * 16u);
 }
+
+// tau with its reciprocal pair for the FP64 collision's divisions (divrn.cuh)
+inline DivRN tau_div(const DomainDev& d) { return make_div_rn(d.tau, 1.0 / d.tau); }
 
 template <class L, class S>
 StepParams<S> step_params(const DomainDev& d)
@@ -39,7 +45,7 @@ StepParams<S> step_params(const DomainDev& d)
     p.err = d.err;
     p.mon = nullptr;
     p.rec = nullptr;
-    p.tau = d.tau;
+    p.tau = tau_div(d);
     p.omega = static_cast<float>(1.0 / d.tau);
     return p;
 }
@@ -88,16 +94,18 @@ struct Launch {
         S* pop = static_cast<S*>(d.pop);
         if (d.n_gf > 0)
             ghost_fluid_kernel<L, S><<<(d.n_gf + 127) / 128, 128, 0, s>>>(
-                pop, d.flag, d.g, d.tau, d.gf_xyz, d.gf_pop, d.n_gf, copy);
+                pop, d.flag, d.g, tau_div(d), d.gf_xyz, d.gf_pop, d.n_gf, copy);
         if (d.n_fs > 0)
             free_slip_kernel<L, S><<<(d.n_fs + 127) / 128, 128, 0, s>>>(
                 pop, d.flag, d.g, d.fs_link, d.n_fs, copy, d.gf_pop, d.n_gf, copy);
     }
 
-    static void step(const DomainDev& d, long long t, double* mon_out, void* rec, cudaStream_t s)
+    static void step(const DomainDev& d, long long t, int mon_set, double* prev_out, void* rec, cudaStream_t s)
     {
         StepParams<S> p = step_params<L, S>(d);
-        p.mon = mon_out ? d.mon : nullptr;
+        p.mon = mon_set >= 0 ? d.mon + 4 * kMonBuckets * mon_set : nullptr;
+        p.mon_prev = mon_set >= 0 && prev_out ? d.mon + 4 * kMonBuckets * (1 - mon_set) : nullptr;
+        p.mon_prev_out = prev_out;
         p.rec = static_cast<typename Store<S>::C*>(rec);
         const int nseg_x = (d.g.xl + kRowCells - 1) / kRowCells;
         const int nseg = nseg_x * d.g.yl * d.g.zl;
@@ -115,20 +123,23 @@ struct Launch {
         const FastDiv fy = make_fastdiv(static_cast<uint32_t>(d.g.yl));
         constexpr size_t smem = row_smem_bytes<L, S>();
         if constexpr (smem > 48 * 1024) {  // only with more than one segment per block
-            // once per process (a thread-safe static initialisation)
-            static const bool opted_in = [] {
+            // the opt-in applies to the current device: once per device and kernel set
+            static std::mutex m;
+            static bool opted_in[kMaxDevices] = {};
+            int dev = 0;
+            cudaGetDevice(&dev);
+            std::lock_guard<std::mutex> lock(m);
+            if (dev >= 0 && dev < kMaxDevices && !opted_in[dev]) {
                 for (auto k : {step_kernel<L, S, true, false>, step_kernel<L, S, false, false>,
                                step_kernel<L, S, true, true>, step_kernel<L, S, false, true>})
                     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-                return true;
-            }();
-            (void)opted_in;
+                opted_in[dev] = true;
+            }
         }
-        const bool instr = mon_out != nullptr || rec != nullptr;
+        const bool instr = mon_set >= 0 || rec != nullptr;
         auto* k = (t & 1) ? (instr ? step_kernel<L, S, true, true> : step_kernel<L, S, true, false>)
                           : (instr ? step_kernel<L, S, false, true> : step_kernel<L, S, false, false>);
         launch_chained(k, dim3(blocks), dim3(kRowCells), smem, s, p, n_edge_blocks, fes, nseg, fx, fy);
-        if (mon_out) monitor_final_kernel<<<1, 256, 0, s>>>(d.mon, mon_out);
         side_passes(d, t, s);
     }
 
@@ -160,6 +171,37 @@ struct Launch {
     {
         moments_kernel<L, S><<<cell_grid(d.g), kBlockX, 0, s>>>(
             static_cast<const S*>(d.pop), d.flag, d.g, static_cast<int>(k & 1), rho, u);
+    }
+
+    static void monitor_fold(const DomainDev& d, int mon_set, double* out, cudaStream_t s)
+    {
+        monitor_fold_kernel<<<1, kMonFoldThreads, 0, s>>>(d.mon + 4 * kMonBuckets * mon_set, out);
+    }
+
+    static void gather_range(const DomainDev& d, long long k, size_t r0, size_t r1, double* out, cudaStream_t s)
+    {
+        gather_range_kernel<L, S><<<linear_blocks(r1 - r0, 256), 256, 0, s>>>(
+            static_cast<const S*>(d.pop), d.flag, d.g, static_cast<int>(k & 1), r0, r1, out);
+    }
+
+    static void scatter_range(const DomainDev& d, long long k, size_t r0, size_t r1, const double* in, cudaStream_t s)
+    {
+        scatter_range_kernel<L, S><<<linear_blocks(r1 - r0, 256), 256, 0, s>>>(
+            static_cast<S*>(d.pop), d.flag, d.g, static_cast<int>(k & 1), r0, r1, in);
+    }
+
+    static void moments_range(const DomainDev& d, long long k, size_t n0, size_t n1, double* rho, double* u,
+                              cudaStream_t s)
+    {
+        moments_range_kernel<L, S><<<linear_blocks(n1 - n0, 256), 256, 0, s>>>(
+            static_cast<const S*>(d.pop), d.flag, d.g, static_cast<int>(k & 1), n0, n1, rho, u);
+    }
+
+    static void ghost_fluid_slots(const DomainDev& d, long long k, cudaStream_t s)
+    {
+        if (d.n_gf > 0)
+            ghost_fluid_slots_kernel<L, S><<<(d.n_gf + 127) / 128, 128, 0, s>>>(
+                static_cast<S*>(d.pop), d.flag, d.g, d.gf_xyz, d.gf_pop, d.n_gf, static_cast<int>(k & 1));
     }
 
     static void reduce(const DomainDev& d, long long k, double* partials, int nblocks,
@@ -215,9 +257,10 @@ struct Launch {
 
     static const KernelOps* table()
     {
-        static const KernelOps t = {&init,     &classify, &step,         &gather,   &scatter,
-                                    &moments,  &reduce,   sizeof(T),     &adj_terminal, &adj_step,
-                                    &link_table, &objective_ke};
+        static const KernelOps t = {&init,         &classify,      &step,          &monitor_fold, &gather,
+                                    &scatter,      &moments,       &gather_range,  &scatter_range,
+                                    &moments_range, &ghost_fluid_slots, &reduce,   sizeof(T),
+                                    &adj_terminal, &adj_step,      &link_table,    &objective_ke};
         return &t;
     }
 };

@@ -168,6 +168,123 @@ __global__ void scatter_kernel(S* pop, const uint8_t* flag, Geom g, int odd, con
     }
 }
 
+// Stores the value that non-fluid cell b = (bx, by, bz) hands to its fluid neighbour n = b + c_q
+// (layout index n), where n pulls it next step: after an odd step plane q at n, after an even
+// step plane inv(q) at b.
+template <class L, class S>
+__device__ __forceinline__ void store_slot(S* pop, const Geom& g, int odd, int n, int bx, int by, int bz, int q,
+                                           typename Store<S>::C v)
+{
+    if (odd)
+        Store<S>::st(pop + static_cast<size_t>(q) * g.PS + n, v);
+    else
+        Store<S>::st(pop + static_cast<size_t>(L::Q - 1 - q) * g.PS + cidx(g, bx, by, bz), v);
+}
+
+// Cell (x, y, z) of row r of the reference's cell order (domain.hpp:60-64).
+__device__ __forceinline__ void ref_xyz(const Geom& g, size_t r, int& x, int& y, int& z)
+{
+    const size_t nx = static_cast<size_t>(g.xl + 2), nxy = nx * static_cast<size_t>(g.yl + 2);
+    z = static_cast<int>(r / nxy);
+    const size_t t = r - static_cast<size_t>(z) * nxy;
+    y = static_cast<int>(t / nx);
+    x = static_cast<int>(t - static_cast<size_t>(y) * nx);
+}
+
+__device__ __forceinline__ bool on_periodic_ghost(const Geom& g, int x, int y, int z)
+{
+    return ((g.per & 1) && (x == 0 || x == g.xl + 1)) || ((g.per & 2) && (y == 0 || y == g.yl + 1)) ||
+           ((g.per & 4) && (z == 0 || z == g.zl + 1));
+}
+
+// Rows [r0, r1) of the AoS FP64 field (reference cell order) from the device layout, row r into
+// out[(r - r0) * Q ..]: one chunk of a read-back through the handle's staging buffers. Ghost-fluid
+// cells come out as w_q; the host writes their side copies over them.
+template <class L, class S>
+__global__ void gather_range_kernel(const S* pop, const uint8_t* flag, Geom g, int odd, size_t r0, size_t r1,
+                                    double* out)
+{
+    for (size_t r = r0 + blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; r < r1;
+         r += static_cast<size_t>(gridDim.x) * blockDim.x) {
+        int x, y, z;
+        ref_xyz(g, r, x, y, z);
+        double f[L::Q];
+        load_cell_f64<L, S>(pop, flag, g, x, y, z, odd != 0, f);
+        double* o = out + (r - r0) * L::Q;
+#pragma unroll
+        for (int q = 0; q < L::Q; ++q) o[q] = f[q];
+    }
+}
+
+// Rows [r0, r1) of the AoS FP64 field (row r at in[(r - r0) * Q ..]) into the device layout with
+// the given parity: one chunk of an upload. An interior fluid cell writes its own post-collision
+// slots; a handler cell writes, for each direction q whose neighbour b + c_q is an interior fluid
+// cell, the slot that neighbour pulls from it (the value its handler wrote in the reference's
+// collide_field). Ghost-fluid cells are written from their side copies afterwards
+// (ghost_fluid_slots_kernel); cells on the ghost planes of periodic axes are never read.
+template <class L, class S>
+__global__ void scatter_range_kernel(S* pop, const uint8_t* flag, Geom g, int odd, size_t r0, size_t r1,
+                                     const double* in)
+{
+    for (size_t r = r0 + blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; r < r1;
+         r += static_cast<size_t>(gridDim.x) * blockDim.x) {
+        int x, y, z;
+        ref_xyz(g, r, x, y, z);
+        const int i = cidx(g, x, y, z);
+        const uint8_t fl = flag[i];
+        const double* row = in + (r - r0) * L::Q;
+        if (is_fluid(fl) && interior(g, x, y, z)) {
+#pragma unroll
+            for (int p = 0; p < L::Q; ++p) {
+                const auto v = from_f64<L, S>(row[p], p);
+                if (!odd) {
+                    Store<S>::st(pop + static_cast<size_t>(inv<L>(p)) * g.PS + i, v);
+                } else {
+                    int mx, my, mz;
+                    nbr_xyz(g, x, y, z, L::c(p, 0), L::c(p, 1), L::c(p, 2), mx, my, mz);
+                    Store<S>::st(pop + static_cast<size_t>(p) * g.PS + cidx(g, mx, my, mz), v);
+                }
+            }
+        } else if (fl >= kFirstHandler && !on_periodic_ghost(g, x, y, z)) {
+#pragma unroll
+            for (int q = 0; q < L::Q; ++q) {
+                int nx, ny, nz;
+                nbr_xyz(g, x, y, z, L::c(q, 0), L::c(q, 1), L::c(q, 2), nx, ny, nz);
+                if (!interior(g, nx, ny, nz)) continue;
+                const int n = cidx(g, nx, ny, nz);
+                if (!is_fluid(flag[n])) continue;
+                store_slot<L, S>(pop, g, odd, n, x, y, z, q, from_f64<L, S>(row[q], q));
+            }
+        }
+    }
+}
+
+// Density and velocity of the interior cells [n0, n1) of the interior order (vtk.hpp:62-73 ->
+// collision.hpp:6-31), FP64: rho_out[n - n0] and u_out[3 (n - n0) ..]; one chunk of lbm_moments.
+template <class L, class S>
+__global__ void moments_range_kernel(const S* pop, const uint8_t* flag, Geom g, int odd, size_t n0, size_t n1,
+                                     double* rho_out, double* u_out)
+{
+    const size_t nx = static_cast<size_t>(g.xl), nxy = nx * static_cast<size_t>(g.yl);
+    for (size_t n = n0 + blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; n < n1;
+         n += static_cast<size_t>(gridDim.x) * blockDim.x) {
+        const int z = static_cast<int>(n / nxy);
+        const size_t t = n - static_cast<size_t>(z) * nxy;
+        const int y = static_cast<int>(t / nx);
+        const int x = static_cast<int>(t - static_cast<size_t>(y) * nx);
+        double f[L::Q];
+        load_cell_f64<L, S>(pop, flag, g, x + 1, y + 1, z + 1, odd != 0, f);
+        const double rho = density_exact<L>(f);
+        const size_t o = n - n0;
+        rho_out[o] = rho;
+        if (u_out) {
+            u_out[3 * o + 0] = momentum_exact<L>(f, 0) / rho;
+            u_out[3 * o + 1] = momentum_exact<L>(f, 1) / rho;
+            u_out[3 * o + 2] = momentum_exact<L>(f, 2) / rho;
+        }
+    }
+}
+
 // Density and velocity of interior cells (vtk.hpp:62-73 -> collision.hpp:6-31), FP64, written
 // as rho[n] and u[3n..3n+2] in interior order.
 template <class L, class S>
@@ -233,20 +350,6 @@ __global__ void __launch_bounds__(kReduceThreads)
     }
 }
 
-// Sums the step monitor's accumulator buckets in a fixed order into out[4] and clears them for the
-// next step.
-static __global__ void monitor_final_kernel(double* buckets, double* out)
-{
-    const int k = static_cast<int>(threadIdx.x);
-    if (k < 4) {
-        double v = 0.0;
-        for (int b = 0; b < kMonBuckets; ++b) v += buckets[4 * b + k];
-        out[k] = v;
-    }
-    __syncthreads();
-    for (int j = k; j < 4 * kMonBuckets; j += blockDim.x) buckets[j] = 0.0;
-}
-
 static __global__ void reduce_final_kernel(const double* partials, int nblocks, double* out)
 {
     if (threadIdx.x < 4) {
@@ -263,21 +366,8 @@ static __global__ void reduce_final_kernel(const double* partials, int nblocks, 
 // is collided at step t. Interior fluid cells pull from them. Copy (t mod 2) is collided after
 // step t and written into the boundary slots of the neighbours, which pull it at step t + 1.
 // ------------------------------------------------------------------------------------------
-// Stores the value that non-fluid cell b = (bx, by, bz) hands to its fluid neighbour n = b + c_q
-// (layout index n), where n pulls it next step: after an odd step plane q at n, after an even
-// step plane inv(q) at b.
 template <class L, class S>
-__device__ __forceinline__ void store_slot(S* pop, const Geom& g, int odd, int n, int bx, int by, int bz, int q,
-                                           typename Store<S>::C v)
-{
-    if (odd)
-        Store<S>::st(pop + static_cast<size_t>(q) * g.PS + n, v);
-    else
-        Store<S>::st(pop + static_cast<size_t>(L::Q - 1 - q) * g.PS + cidx(g, bx, by, bz), v);
-}
-
-template <class L, class S>
-__global__ void ghost_fluid_kernel(S* pop, const uint8_t* flag, Geom g, double tau,
+__global__ void ghost_fluid_kernel(S* pop, const uint8_t* flag, Geom g, DivRN tau,
                                    const int* gf_xyz, double* gf_pop, int n_gf, int copy)
 {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
