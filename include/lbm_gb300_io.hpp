@@ -4,6 +4,8 @@
 //   parse_scenario_file    io/scenario.h:131-188       XML scenario -> Domain
 //   read_vtk_point_file    io/vtk.hpp:93-157           legacy-VTK fluid mask -> Domain
 //   write_vtk_file         io/vtk.hpp:42-89            <dir>/<name>.<t>.vts from device moments
+//   VtkWriter              (extension)                 the same files, written on a background
+//                                                      thread while the time loop runs on
 //
 // No boost, pugixml or VTK: the config file, the XML subset the scenarios use (prolog, comments,
 // elements, quoted attributes) and the legacy STRUCTURED_POINTS format are parsed here, and the
@@ -13,17 +15,22 @@
 #pragma once
 
 #include <cctype>
+#include <condition_variable>
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <deque>
+#include <exception>
 #include <filesystem>
 #include <fstream>
 #include <iostream>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <sstream>
 #include <stdexcept>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "lbm_gb300.hpp"
@@ -496,29 +503,47 @@ inline std::string base64_block(const void* data, uint32_t nbytes)
 }
 }  // namespace detail_vts
 
-// <output_dir>/<output_filename>.<t>.vts: point data "Velocity" (3 x Float64) and "Density"
-// (Float64) of the interior cells, x fastest, at points (xs*x + xo - 1, ys*y + yo - 1,
-// zs*z + zo - 1), x = 1..xl etc. (Float32). The moments come from the device.
-template <typename lattice_model>
-void write_vtk_file(const Domain<lattice_model>& domain, const std::string& output_dir,
-                    const std::string& output_filename, uint64_t t)
-{
-    const size_t xl = domain.xlength(), yl = domain.ylength(), zl = domain.zlength();
+// One output file's data: the moments of the interior cells at one step, read from the device,
+// and what the file names and places.
+struct VtsSnapshot {
+    size_t xl = 0, yl = 0, zl = 0;
+    double xo = 0, yo = 0, zo = 0, xs = 1, ys = 1, zs = 1;
     std::vector<double> rho, u;
-    domain.moments(rho, u);
+    std::string path;
+};
+
+template <typename lattice_model>
+VtsSnapshot vts_snapshot(const Domain<lattice_model>& domain, const std::string& output_dir,
+                         const std::string& output_filename, uint64_t t)
+{
+    VtsSnapshot s;
+    s.xl = domain.xlength(), s.yl = domain.ylength(), s.zl = domain.zlength();
+    s.xo = domain.xorigin(), s.yo = domain.yorigin(), s.zo = domain.zorigin();
+    s.xs = domain.xspacing(), s.ys = domain.yspacing(), s.zs = domain.zspacing();
+    domain.moments(s.rho, s.u);
+    std::ostringstream name;
+    name << output_dir << "/" << output_filename << "." << t << ".vts";
+    s.path = name.str();
+    return s;
+}
+
+// The file of a snapshot: point data "Velocity" (3 x Float64) and "Density" (Float64) of the
+// interior cells, x fastest, at points (xs*x + xo - 1, ys*y + yo - 1, zs*z + zo - 1), x = 1..xl
+// etc. (Float32).
+inline void write_vts(const VtsSnapshot& s)
+{
+    const size_t xl = s.xl, yl = s.yl, zl = s.zl;
     std::vector<float> pts(3 * xl * yl * zl);
     size_t k = 0;
     for (size_t z = 1; z <= zl; ++z)
         for (size_t y = 1; y <= yl; ++y)
             for (size_t x = 1; x <= xl; ++x) {
-                pts[k++] = static_cast<float>(domain.xspacing() * x + domain.xorigin() - 1);
-                pts[k++] = static_cast<float>(domain.yspacing() * y + domain.yorigin() - 1);
-                pts[k++] = static_cast<float>(domain.zspacing() * z + domain.zorigin() - 1);
+                pts[k++] = static_cast<float>(s.xs * x + s.xo - 1);
+                pts[k++] = static_cast<float>(s.ys * y + s.yo - 1);
+                pts[k++] = static_cast<float>(s.zs * z + s.zo - 1);
             }
-    std::ostringstream name;
-    name << output_dir << "/" << output_filename << "." << t << ".vts";
-    std::ofstream file(name.str(), std::ios::trunc | std::ios::binary);
-    if (!file) throw std::logic_error("Failed to open file " + name.str());
+    std::ofstream file(s.path, std::ios::trunc | std::ios::binary);
+    if (!file) throw std::logic_error("Failed to open file " + s.path);
     const std::string ext = "0 " + std::to_string(xl - 1) + " 0 " + std::to_string(yl - 1) + " 0 " +
                             std::to_string(zl - 1);
     using detail_vts::base64_block;
@@ -528,10 +553,10 @@ void write_vtk_file(const Domain<lattice_model>& domain, const std::string& outp
          << "    <Piece Extent=\"" << ext << "\">\n"
          << "      <PointData Scalars=\"Density\" Vectors=\"Velocity\">\n"
          << "        <DataArray type=\"Float64\" Name=\"Velocity\" NumberOfComponents=\"3\" format=\"binary\">\n"
-         << base64_block(u.data(), static_cast<uint32_t>(u.size() * sizeof(double))) << "\n"
+         << base64_block(s.u.data(), static_cast<uint32_t>(s.u.size() * sizeof(double))) << "\n"
          << "        </DataArray>\n"
          << "        <DataArray type=\"Float64\" Name=\"Density\" format=\"binary\">\n"
-         << base64_block(rho.data(), static_cast<uint32_t>(rho.size() * sizeof(double))) << "\n"
+         << base64_block(s.rho.data(), static_cast<uint32_t>(s.rho.size() * sizeof(double))) << "\n"
          << "        </DataArray>\n"
          << "      </PointData>\n"
          << "      <CellData></CellData>\n"
@@ -543,8 +568,104 @@ void write_vtk_file(const Domain<lattice_model>& domain, const std::string& outp
          << "    </Piece>\n"
          << "  </StructuredGrid>\n"
          << "</VTKFile>\n";
-    if (!file) throw std::logic_error("Failed to write file " + name.str());
+    if (!file) throw std::logic_error("Failed to write file " + s.path);
 }
+
+// vtk.hpp:42-89: <output_dir>/<output_filename>.<t>.vts from the device moments, written on the
+// caller's thread.
+template <typename lattice_model>
+void write_vtk_file(const Domain<lattice_model>& domain, const std::string& output_dir,
+                    const std::string& output_filename, uint64_t t)
+{
+    write_vts(vts_snapshot(domain, output_dir, output_filename, t));
+}
+
+// Extension: the reference writes every file on the time loop's thread (main.cpp:56-57), so the
+// solver waits while the moments are encoded and written. submit() reads the moments from the
+// device (one synchronising read-back) and hands the file to a background thread; the loop then
+// goes on launching steps while the file is written. At most `depth` snapshots wait in host memory
+// (submit blocks beyond that). A failed write is rethrown by the next submit() or by finish();
+// the destructor finishes the queue and drops any error.
+class VtkWriter {
+public:
+    explicit VtkWriter(size_t depth = 2) : depth_(depth ? depth : 1), worker_([this] { run(); }) {}
+    VtkWriter(const VtkWriter&) = delete;
+    VtkWriter& operator=(const VtkWriter&) = delete;
+    ~VtkWriter()
+    {
+        try {
+            finish();
+        } catch (...) {
+        }
+        {
+            std::lock_guard<std::mutex> lock(m_);
+            stop_ = true;
+        }
+        cv_.notify_all();
+        worker_.join();
+    }
+
+    template <typename lattice_model>
+    void submit(const Domain<lattice_model>& domain, const std::string& output_dir,
+                const std::string& output_filename, uint64_t t)
+    {
+        VtsSnapshot s = vts_snapshot(domain, output_dir, output_filename, t);
+        std::unique_lock<std::mutex> lock(m_);
+        rethrow_locked();
+        cv_.wait(lock, [this] { return queue_.size() < depth_; });
+        queue_.push_back(std::move(s));
+        cv_.notify_all();
+    }
+
+    // Waits until every submitted file is written; rethrows the first failure.
+    void finish()
+    {
+        std::unique_lock<std::mutex> lock(m_);
+        cv_.wait(lock, [this] { return queue_.empty() && !busy_; });
+        rethrow_locked();
+    }
+
+private:
+    void rethrow_locked()
+    {
+        if (error_) {
+            std::exception_ptr e = error_;
+            error_ = nullptr;
+            std::rethrow_exception(e);
+        }
+    }
+    void run()
+    {
+        std::unique_lock<std::mutex> lock(m_);
+        for (;;) {
+            cv_.wait(lock, [this] { return stop_ || !queue_.empty(); });
+            if (queue_.empty()) return;  // stop requested and nothing left
+            VtsSnapshot s = std::move(queue_.front());
+            queue_.pop_front();
+            busy_ = true;
+            lock.unlock();
+            try {
+                write_vts(s);
+            } catch (...) {
+                lock.lock();
+                if (!error_) error_ = std::current_exception();
+                lock.unlock();
+            }
+            lock.lock();
+            busy_ = false;
+            cv_.notify_all();
+        }
+    }
+
+    size_t depth_;
+    std::mutex m_;
+    std::condition_variable cv_;
+    std::deque<VtsSnapshot> queue_;
+    bool busy_ = false;
+    bool stop_ = false;
+    std::exception_ptr error_;
+    std::thread worker_;
+};
 
 }  // namespace io
 }  // namespace lbm

@@ -93,7 +93,7 @@ def build_driver(lib: Path = LIB) -> Path:
     if DRIVER.exists() and DRIVER.stat().st_mtime >= max(p.stat().st_mtime for p in deps):
         return DRIVER
     cmd = [cxx, "-std=c++17", "-O2", "-Wall", "-Wextra", "-I", str(INCLUDE), str(DRIVER_SRC), "-o", str(DRIVER),
-           "-L", str(lib.parent), "-llbm_gb300", "-Wl,-rpath,$ORIGIN"]
+           "-L", str(lib.parent), "-llbm_gb300", "-Wl,-rpath,$ORIGIN", "-pthread"]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"driver build failed:\n{res.stdout}\n{res.stderr}")

@@ -333,8 +333,78 @@ def write_vtk_file(domain, output_dir, output_filename: str, t: int, binary: boo
     """vtk.hpp:42-89: <output_dir>/<output_filename>.<t>.vts from the domain's moments (computed on
     the device)."""
     rho, u = domain.moments()
+    path = Path(output_dir) / f"{output_filename}.{t}.vts"
+    _write_vts(path, domain, rho, u, binary)
+    return path
+
+
+def _write_vts(path: Path, domain, rho, u, binary: bool) -> None:
     doc = vts_document(domain.xl, domain.yl, domain.zl, (domain.xo, domain.yo, domain.zo),
                        (domain.xs, domain.ys, domain.zs), rho, u, binary)
-    path = Path(output_dir) / f"{output_filename}.{t}.vts"
     path.write_text(doc)
-    return path
+
+
+class _DomainGeometry:
+    """The sizes, origin and spacing of a domain: what a queued file needs after the loop moved on."""
+
+    def __init__(self, d):
+        self.xl, self.yl, self.zl = d.xl, d.yl, d.zl
+        self.xo, self.yo, self.zo = d.xo, d.yo, d.zo
+        self.xs, self.ys, self.zs = d.xs, d.ys, d.zs
+
+
+class VtkWriter:
+    """Extension: write_vtk_file with the file written on a background thread. The reference writes
+    on the time loop's thread (main.cpp:56-57); here submit() reads the moments back (one
+    synchronising read) and returns, and the loop keeps launching steps while the file is encoded
+    and written. At most `depth` snapshots wait in memory; a failed write is raised by the next
+    submit() or by finish()."""
+
+    def __init__(self, depth: int = 2):
+        import queue
+        import threading
+        self._q = queue.Queue(maxsize=max(1, depth))
+        self._error = None
+        self._thread = threading.Thread(target=self._run, daemon=True)
+        self._thread.start()
+
+    def _run(self):
+        while True:
+            job = self._q.get()
+            try:
+                if job is None:
+                    return
+                _write_vts(*job)
+            except BaseException as e:  # kept for the caller's thread
+                if self._error is None:
+                    self._error = e
+            finally:
+                self._q.task_done()
+
+    def _raise(self):
+        if self._error is not None:
+            e, self._error = self._error, None
+            raise e
+
+    def submit(self, domain, output_dir, output_filename: str, t: int, binary: bool = True) -> Path:
+        self._raise()
+        rho, u = domain.moments()
+        path = Path(output_dir) / f"{output_filename}.{t}.vts"
+        self._q.put((path, _DomainGeometry(domain), rho, u, binary))
+        return path
+
+    def finish(self) -> None:
+        """Waits for every submitted file; raises the first failure."""
+        self._q.join()
+        self._raise()
+
+    def close(self) -> None:
+        self.finish()
+        self._q.put(None)
+        self._thread.join()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()

@@ -99,6 +99,24 @@ def test_scenario_file_config_and_vts_output(tmp_path):
     assert sorted(p.name for p in (tmp_path / "vtk").iterdir()) == ["Backward step.10.vts", "Backward step.20.vts"]
 
 
+def test_background_vts_writer_matches_direct_files(tmp_path):
+    # io.VtkWriter writes the same files as write_vtk_file, on a background thread while the loop
+    # keeps stepping
+    scn = io.parse_scenario(STEP_XML, q=19, tau=0.6)
+    from lbm_gb300 import build_domain
+    with build_domain(scn, "fp32") as dom, io.VtkWriter(depth=2) as w:
+        paths = []
+        for t in range(1, 31):
+            dom.step(1)
+            if t % 10 == 0:
+                paths.append(w.submit(dom, tmp_path, "bg", t))
+                io.write_vtk_file(dom, tmp_path, "direct", t)
+        w.finish()
+    assert [p.name for p in paths] == ["bg.10.vts", "bg.20.vts", "bg.30.vts"]
+    for t in (10, 20, 30):
+        assert (tmp_path / f"bg.{t}.vts").read_bytes() == (tmp_path / f"direct.{t}.vts").read_bytes()
+
+
 def test_read_vtk_point_file_domain(tmp_path):
     mask = tube_mask(10, 7, 6, 2.2)
     write_mask_vtk(tmp_path / "m.vtk", mask, origin=(1.0, 2.0, 3.0), spacing=(0.5, 0.5, 0.5))

@@ -239,3 +239,34 @@ def test_driver_scenario_errors(driver, tmp_path):
     r = _run(driver, ["--tau", "0.6", "-t", "2", "--timesteps-per-plot", "0", "--scenario-file", "none.xml",
                       "--output-dir", str(tmp_path / "o")], tmp_path)
     assert 'XML file "none.xml" could not be read properly!' in r.stderr
+
+
+class _FakeDomain:
+    """Sizes, placement and moments of a domain, without a GPU (for the writers' host logic)."""
+
+    def __init__(self, xl=5, yl=4, zl=3, seed=0):
+        self.xl, self.yl, self.zl = xl, yl, zl
+        self.xo, self.yo, self.zo = 0.5, -1.0, 2.0
+        self.xs, self.ys, self.zs = 2.0, 1.0, 0.25
+        rng = np.random.default_rng(seed)
+        self.rho = 1 + 0.01 * rng.standard_normal((zl, yl, xl))
+        self.u = 0.05 * rng.standard_normal((zl, yl, xl, 3))
+
+    def moments(self):
+        return self.rho.copy(), self.u.copy()
+
+
+def test_background_vts_writer_host_logic(tmp_path):
+    dom = _FakeDomain()
+    with io.VtkWriter(depth=1) as w:
+        for t in (1, 2, 3):
+            dom.rho += 0.001  # the loop moves on: each file keeps its own snapshot
+            w.submit(dom, tmp_path, "bg", t)
+            io.write_vtk_file(dom, tmp_path, "direct", t)
+    for t in (1, 2, 3):
+        assert (tmp_path / f"bg.{t}.vts").read_bytes() == (tmp_path / f"direct.{t}.vts").read_bytes()
+    w = io.VtkWriter()
+    w.submit(dom, tmp_path / "missing-dir", "x", 1)
+    with pytest.raises(OSError):
+        w.finish()
+    w.close()
