@@ -180,7 +180,9 @@ __device__ __forceinline__ double feq_exact(int q, double rho, double u0, double
 __device__ __forceinline__ void velocity_exact(const double (&m)[4], double& u0, double& u1, double& u2)
 {
     const double rho = m[0];
-    if (rho >= 0x1p-30 && rho <= 0x1p+30) {
+    uint32_t hi, lo;
+    words(rho, hi, lo);
+    if (hi - 0x3e100000u < 0x41d00000u - 0x3e100000u) {  // 2^-30 <= rho < 2^30 (integer test)
         const DivRN r = make_div_rn(rho, __drcp_rn(rho));
         u0 = div_rn(m[1], r);
         u1 = div_rn(m[2], r);
@@ -529,7 +531,7 @@ __device__ __forceinline__ void store_edge_populations(const StepParams<S>& P, i
 
 // The step kernel, one launch per time step, with two kinds of blocks.
 //
-// Row blocks update the bulk and wall cells (kFluidBulk, kFluidWall) of kSegs consecutive
+// Row blocks update the bulk and wall cells (kFluidBulk, kFluidWall) of segs<S>() consecutive
 // segments of kRowCells cells of x-rows, one thread per cell:
 // - At the start the first warp brings the Q source rows of every segment into the segment's own
 //   shared-memory stage with bulk asynchronous copies (TMA), one copy per lane, each stage
@@ -549,11 +551,20 @@ __device__ __forceinline__ void store_edge_populations(const StepParams<S>& P, i
 #ifndef LBMG_ROW_CELLS
 #define LBMG_ROW_CELLS 128
 #endif
-#ifndef LBMG_SEGS
-#define LBMG_SEGS 1
-#endif
 constexpr int kRowCells = LBMG_ROW_CELLS;
-constexpr int kSegs = LBMG_SEGS;
+// Segments per row block: a block with two segments issues the copies of both at its start, so the
+// second segment's rows land while the first one is computed. That pays for 16-bit storage (the
+// 256x128x128 D3Q19 channel in FP16: 49.8k against 46.6k MLUPS) and not for FP32 (35.9k against
+// 36.4k). LBMG_SEGS sets every storage type in tuning builds.
+template <class S>
+constexpr int segs()
+{
+#ifdef LBMG_SEGS
+    return LBMG_SEGS;
+#else
+    return sizeof(S) == 2 ? 2 : 1;
+#endif
+}
 constexpr int kMonFoldThreads = kRowCells;  // threads of a step-kernel block
 constexpr uint32_t kMaxPolls = 1u << 20;
 // Polls of a row block's first wait for its staged rows. The failure tests build a copy of the
@@ -565,31 +576,57 @@ constexpr uint32_t kMaxPolls = 1u << 20;
 #endif
 constexpr uint32_t kRowWaitPolls = LBMG_ROW_WAIT_POLLS;
 
+// Waits for a segment's staged rows. With LBMG_WARP_WAIT, lane 0 of each warp polls the barrier
+// while the other lanes wait at __syncwarp (issuing nothing); each of them then tests the barrier
+// once, which gives it the acquire ordering of the completed phase (or tells it the wait gave up).
+#ifndef LBMG_WARP_WAIT
+#define LBMG_WARP_WAIT 0
+#endif
+__device__ __forceinline__ bool row_wait(uint64_t* bar)
+{
+#if LBMG_WARP_WAIT
+    bool ok = false;
+    if ((threadIdx.x & 31) == 0) ok = mbar_wait_bounded(bar, 0, kRowWaitPolls);
+    __syncwarp();
+    return ((threadIdx.x & 31) == 0) ? ok : mbar_test_wait(bar, 0);
+#else
+    return mbar_wait_bounded(bar, 0, kRowWaitPolls);
+#endif
+}
+
 template <class S>
 constexpr int row_pad()
 {
     return static_cast<int>(16 / sizeof(S));
 }
-// one stage: the widened rows of a segment, or (edge blocks) the handler scratch
+// one row-block stage: the widened rows of a segment
 template <class L, class S>
 constexpr size_t stage_bytes()
 {
     const size_t rows = static_cast<size_t>(L::Q) * (kRowCells + 2 * row_pad<S>()) * sizeof(S);
-    const size_t scratch = static_cast<size_t>(L::Q) * kRowCells * sizeof(typename Store<S>::C);
-    const size_t m = rows > scratch ? rows : scratch;
-    return (m + 127) / 128 * 128;
+    return (rows + 127) / 128 * 128;
 }
-// Shared memory of a row block: the staged rows, then (shifted storage) one LinkRecord per thread
-// (48 bytes, 16-byte aligned: the destination of its cp.async copies).
+// an edge block's handler scratch: the post-collision populations of its cells
+template <class L, class S>
+constexpr size_t edge_scratch_bytes()
+{
+    return static_cast<size_t>(L::Q) * kRowCells * sizeof(typename Store<S>::C);
+}
+// (shifted storage) one LinkRecord per thread (64 bytes, 16-byte aligned: the destination of its
+// cp.async copies)
 template <class S>
 constexpr size_t link_smem_bytes()
 {
     return Store<S>::kShifted ? static_cast<size_t>(kLinkWords) * kRowCells * 4 : 0;
 }
+// Dynamic shared memory of a step-kernel block: a row block's stages and then its LinkRecords, or
+// an edge block's scratch from the start, whichever is larger.
 template <class L, class S>
 constexpr size_t row_smem_bytes()
 {
-    return kSegs * stage_bytes<L, S>() + link_smem_bytes<S>();
+    const size_t rows = segs<S>() * stage_bytes<L, S>() + link_smem_bytes<S>();
+    const size_t edge = edge_scratch_bytes<L, S>();
+    return rows > edge ? rows : edge;
 }
 
 // Step monitor. Each block adds the moments its cells started from (m as collide_any returns them,
@@ -826,6 +863,7 @@ __device__ __forceinline__ void row_block(const StepParams<S>& P, int rb, int ns
     const int tx = static_cast<int>(threadIdx.x);
     const size_t PS = P.g.PS;
     S* __restrict__ pop = P.pop;
+    constexpr int kSegs = segs<S>();
     const int seg0 = rb * kSegs;
     const int nsegs = nseg - seg0 < kSegs ? nseg - seg0 : kSegs;
 
@@ -883,7 +921,7 @@ __device__ __forceinline__ void row_block(const StepParams<S>& P, int rb, int ns
                 cp_async_commit();
             }
         }
-        if (!mbar_wait_bounded(&bars[s], 0, kRowWaitPolls)) {
+        if (!row_wait(&bars[s])) {
             // the step's results are invalid; still never leave while copies may land here (this
             // drain wait is bounded too: if it also gives up the block returns regardless)
             *P.err = 1;
@@ -948,8 +986,10 @@ constexpr int min_blocks()
 #if defined(LBMG_MINB_EVEN)
         if (!ODD) return LBMG_MINB_EVEN;
 #endif
-        // the instrumented D3Q15 kernels (monitor, adjoint record) would spill at 40 registers
+        // the instrumented kernels (monitor, adjoint record) would spill at the plain kernels'
+        // bounds: D3Q15 at 40 registers, 16-bit D3Q19 with two segments per block at 48
         if (INSTR && L::Q == 15) return 10;
+        if (INSTR && L::Q == 19 && sizeof(S) == 2) return 9;
         return L::Q == 19 ? 10 : L::Q == 27 ? LBMG_MINB_Q27 : LBMG_MINB_Q15;
     }
 }
@@ -969,7 +1009,7 @@ __global__ void __launch_bounds__(kRowCells, min_blocks<L, S, ODD, INSTR>())
     step_kernel(const StepParams<S> P, int n_edge_blocks, FastDiv edge_stride, int nseg, FastDiv nseg_x, FastDiv yl)
 {
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    __shared__ __align__(8) uint64_t bars[kSegs];
+    __shared__ __align__(8) uint64_t bars[segs<S>()];
     // before any global access: the previous step (or whatever kernel precedes this one) has
     // completed; then the next step's blocks may take the SMs this grid's last blocks leave
     grid_dep_wait();

@@ -109,6 +109,7 @@ struct Launch {
         p.rec = static_cast<typename Store<S>::C*>(rec);
         const int nseg_x = (d.g.xl + kRowCells - 1) / kRowCells;
         const int nseg = nseg_x * d.g.yl * d.g.zl;
+        constexpr int kSegs = segs<S>();
         const int row_blocks = (nseg + kSegs - 1) / kSegs;
         const int n_edge_blocks = (d.n_edge + kRowCells - 1) / kRowCells;
         const long long total = static_cast<long long>(n_edge_blocks) + row_blocks;
