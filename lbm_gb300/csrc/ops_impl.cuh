@@ -239,7 +239,8 @@ struct Launch {
         a.write_mu = write_mu;
         a.grad_inflow = grad_inflow;
         a.grad_wall = grad_wall;
-        launch_chained(adjoint_step_kernel<L, T>, cell_grid(d.g), dim3(kBlockX), 0, s, a);
+        a.err = d.err;
+        launch_chained(adjoint_step_kernel<L, T>, cell_grid(d.g), dim3(kBlockX), adj_stage_bytes<L, T>(), s, a);
     }
 
     static void objective_ke(const DomainDev& d, long long k, Box box, double* partials, int nblocks,
