@@ -38,7 +38,6 @@ struct AdjParams {
     int write_mu;         // 0: only the theta gradients of step t
     double* grad_inflow;  // 3 per cell, reference cell order (inflow cells)
     double* grad_wall;    // 3 per handler
-    int* err;             // device error word: set to 1 when a bounded wait gives up
 };
 
 template <class T>
@@ -155,75 +154,23 @@ __device__ __forceinline__ void warp_flush_wall(double* grad_wall, int hid, cons
 #define LBMG_ADJ_MINB 0
 #endif
 
-// Widening of the staged adjoint rows on each side: 16 bytes (the copies' alignment and the +-1
-// shift in x of the transposed pull).
-template <class T>
-constexpr int adj_pad()
-{
-    return static_cast<int>(16 / sizeof(T));
-}
-template <class L, class T>
-constexpr size_t adj_stage_bytes()
-{
-    return static_cast<size_t>(L::Q) * (kBlockX + 2 * adj_pad<T>()) * sizeof(T);
-}
-
-// One block per 128 cells of an x-row (blockIdx.x: the segment, blockIdx.y / z: the row). At the
-// start, lanes 0..Q-1 of the first warp copy the Q rows of mu_t that the segment's transposed pull
-// reads (plane p at row (y + c_p,y, z + c_p,z), widened by 16 bytes on both sides) into shared
-// memory with bulk asynchronous copies on one mbarrier, while every thread loads its flag, link
-// word and recorded moments. The loads in flight are bounded by shared memory, not registers.
 template <class L, class T>
 __global__ void __launch_bounds__(kBlockX, sizeof(T) == 4 ? LBMG_ADJ_MINB : 0) adjoint_step_kernel(const AdjParams<T> A)
 {
     using K = AdjConst<T>;
     constexpr int Q = L::Q;
-    constexpr int PAD = adj_pad<T>();
-    constexpr int W = kBlockX + 2 * PAD;
-    extern __shared__ __align__(128) unsigned char adj_smem[];
-    __shared__ __align__(8) uint64_t bar;
-    T* stage = reinterpret_cast<T*>(adj_smem);
     grid_dep_wait();  // the previous adjoint step (or the kernel before it) has completed
     grid_dep_launch();
-    const int tx = static_cast<int>(threadIdx.x);
-    const int x0 = 1 + static_cast<int>(blockIdx.x) * kBlockX;
-    const int x = x0 + tx;
+    const int x = 1 + static_cast<int>(blockIdx.x) * kBlockX + static_cast<int>(threadIdx.x);
     const int y = 1 + static_cast<int>(blockIdx.y), z = 1 + static_cast<int>(blockIdx.z);
     const int i = cidx(A.g, x, y, z);
-    const size_t PS = A.g.PS;
-    if (tx == 0) {
-        mbar_init(&bar, 1);
-        fence_mbar_init();
-    }
-    __syncthreads();
-    if (tx < 32) {
-        if (tx == 0) mbar_arrive_expect_tx(&bar, Q * W * static_cast<uint32_t>(sizeof(T)));
-        __syncwarp();
-        if (tx < Q) {
-            const int p = tx;
-            const T* src = A.mu_in + static_cast<size_t>(p) * PS +
-                           (static_cast<size_t>(kXOff + x0 - PAD) +
-                            static_cast<size_t>(A.g.XS) *
-                                (static_cast<size_t>(y + rt_c<L>(p, 1)) +
-                                 static_cast<size_t>(A.g.YS) * static_cast<size_t>(z + rt_c<L>(p, 2))));
-            bulk_g2s_hint(stage + p * W, src, W * static_cast<uint32_t>(sizeof(T)), &bar, l2_stream_policy(true));
-        }
-    }
     const uint8_t fl = x <= A.g.xl ? A.flag[i] : static_cast<uint8_t>(0xff);
-    bool active = is_fluid(fl);
+    const bool active = is_fluid(fl);
     int wall_h = -1;               // moving-wall handler whose gradient this thread accumulates
     double gw[3] = {0.0, 0.0, 0.0};
-    const uint2 lw = active && fl != kFluidBulk ? A.link[i] : make_uint2(0u, kNoRecord);
-    T rho_s = T(1), jxs = T(0), jys = T(0), jzs = T(0);
-    if (active) ld_rec4(A.rec + 4 * static_cast<size_t>(i), rho_s, jxs, jys, jzs);
-    if (!mbar_wait_bounded(&bar, 0, kMaxPolls)) {
-        // no result for this step; still never leave while copies may land here (this drain wait
-        // is bounded too)
-        *A.err = 1;
-        mbar_wait_bounded(&bar, 0, kMaxPolls);
-        active = false;
-    }
     if (active) {
+        const size_t PS = A.g.PS;
+        const uint2 lw = fl != kFluidBulk ? A.link[i] : make_uint2(0u, kNoRecord);
         const uint32_t link = lw.x;  // bit q: x - c_q is a boundary cell
         // the links whose handler terms apply this step
         const uint32_t own = A.bc_terms ? link : 0u;
@@ -232,16 +179,22 @@ __global__ void __launch_bounds__(kBlockX, sizeof(T) == 4 ? LBMG_ADJ_MINB : 0) a
         // every adjoint array (cleared once, never written), so no neighbour test is needed. For a
         // link q the pull of direction inv(q) meets such a cell; that slot reads x's own mu_q
         // instead, the quantity every handler term of q starts from (for no-slip, lam[inv q] += mu_q
-        // is the whole term). Bulk and wall cells have no wrapped neighbour, so the staged rows
-        // hold all their pulls.
-        if (fl != kFluidEdge) {
+        // is the whole term). Bulk cells have no wrapped neighbour either.
+        if (fl != kFluidEdge) {  // no wrapped neighbour
+            // one running pointer over the planes (block-uniform deltas), as the step's stores
+            const int sy = A.g.XS, sz = A.g.XS * A.g.YS;
+            const T* ptr = A.mu_in + i + (L::c(0, 0) + L::c(0, 1) * sy + L::c(0, 2) * sz);
 #pragma unroll
             for (int p = 0; p < Q; ++p) {
                 const int qo = Q - 1 - p;  // the link whose pull partner is direction p
-                if ((own >> qo) & 1u)
-                    lam[p] = __ldcs(A.mu_in + static_cast<size_t>(qo) * PS + i);
-                else
-                    lam[p] = stage[p * W + PAD + tx + L::c(p, 0)];
+                const long long self = static_cast<long long>(qo - p) * static_cast<long long>(PS) -
+                                       (L::c(p, 0) + L::c(p, 1) * sy + L::c(p, 2) * sz);
+                lam[p] = __ldcs(((own >> qo) & 1u) ? ptr + self : ptr);
+                if (p + 1 < Q) {
+                    const int d = (L::c(p + 1, 0) - L::c(p, 0)) + (L::c(p + 1, 1) - L::c(p, 1)) * sy +
+                                  (L::c(p + 1, 2) - L::c(p, 2)) * sz;
+                    ptr += static_cast<long long>(PS) + d;
+                }
             }
         } else {
 #pragma unroll
@@ -258,6 +211,8 @@ __global__ void __launch_bounds__(kBlockX, sizeof(T) == 4 ? LBMG_ADJ_MINB : 0) a
                 lam[p] = __ldcs(&A.mu_in[k]);
             }
         }
+        T rho_s, jxs, jys, jzs;
+        ld_rec4(A.rec + 4 * static_cast<size_t>(i), rho_s, jxs, jys, jzs);
         // links whose handler needs its table entry: every link of a kFluidEdge cell; of a
         // kFluidWall cell only those its LinkRecord lists (the others are no-slip, done above)
         uint32_t generic = own;

@@ -239,8 +239,7 @@ struct Launch {
         a.write_mu = write_mu;
         a.grad_inflow = grad_inflow;
         a.grad_wall = grad_wall;
-        a.err = d.err;
-        launch_chained(adjoint_step_kernel<L, T>, cell_grid(d.g), dim3(kBlockX), adj_stage_bytes<L, T>(), s, a);
+        launch_chained(adjoint_step_kernel<L, T>, cell_grid(d.g), dim3(kBlockX), 0, s, a);
     }
 
     static void objective_ke(const DomainDev& d, long long k, Box box, double* partials, int nblocks,
