@@ -576,23 +576,6 @@ constexpr uint32_t kMaxPolls = 1u << 20;
 #endif
 constexpr uint32_t kRowWaitPolls = LBMG_ROW_WAIT_POLLS;
 
-// Waits for a segment's staged rows. With LBMG_WARP_WAIT, lane 0 of each warp polls the barrier
-// while the other lanes wait at __syncwarp (issuing nothing); each of them then tests the barrier
-// once, which gives it the acquire ordering of the completed phase (or tells it the wait gave up).
-#ifndef LBMG_WARP_WAIT
-#define LBMG_WARP_WAIT 0
-#endif
-__device__ __forceinline__ bool row_wait(uint64_t* bar)
-{
-#if LBMG_WARP_WAIT
-    bool ok = false;
-    if ((threadIdx.x & 31) == 0) ok = mbar_wait_bounded(bar, 0, kRowWaitPolls);
-    __syncwarp();
-    return ((threadIdx.x & 31) == 0) ? ok : mbar_test_wait(bar, 0);
-#else
-    return mbar_wait_bounded(bar, 0, kRowWaitPolls);
-#endif
-}
 
 template <class S>
 constexpr int row_pad()
@@ -921,7 +904,7 @@ __device__ __forceinline__ void row_block(const StepParams<S>& P, int rb, int ns
                 cp_async_commit();
             }
         }
-        if (!row_wait(&bars[s])) {
+        if (!mbar_wait_bounded(&bars[s], 0, kRowWaitPolls)) {
             // the step's results are invalid; still never leave while copies may land here (this
             // drain wait is bounded too: if it also gives up the block returns regardless)
             *P.err = 1;

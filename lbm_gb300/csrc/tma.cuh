@@ -71,21 +71,6 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
     return ok != 0;
 }
 
-// Tests once, without waiting, whether phase `parity` of `bar` has completed (with acquire
-// ordering for the calling thread when it has).
-__device__ __forceinline__ bool mbar_test_wait(uint64_t* bar, uint32_t parity)
-{
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-
 // Waits for phase `parity` of `bar` with a bounded number of polls (at most about
 // max_polls * kWaitHintNs). Returns false (and the caller reports an error) if the phase did not
 // complete in time.
