@@ -970,9 +970,9 @@ constexpr int min_blocks()
         if (!ODD) return LBMG_MINB_EVEN;
 #endif
         // the instrumented kernels (monitor, adjoint record) would spill at the plain kernels'
-        // bounds: D3Q15 at 40 registers, 16-bit D3Q19 with two segments per block at 48
+        // bounds: D3Q15 at 40 registers, D3Q19 at 48
         if (INSTR && L::Q == 15) return 10;
-        if (INSTR && L::Q == 19 && sizeof(S) == 2) return 9;
+        if (INSTR && L::Q == 19) return 9;
         return L::Q == 19 ? 10 : L::Q == 27 ? LBMG_MINB_Q27 : LBMG_MINB_Q15;
     }
 }

@@ -316,3 +316,40 @@ def test_chunked_transfers_roundtrip_and_continue(steps_before):
     assert np.array_equal(got[mask], want[mask])
     fl = scn.fluid_mask_interior()
     assert np.array_equal(rho[fl], wr[fl]) and np.array_equal(u[fl], wu[fl])
+
+
+@pytest.mark.parametrize("steps", [1, 2, 21])
+def test_full_row_segments_fp64_vs_port(steps):
+    # 256 cells along x with no-slip walls only: every 128-cell segment is made of bulk and wall
+    # cells, so the step writes through the segment's shared-memory stage and row-wide bulk copies
+    # (the unaligned ends of the odd steps' shifted rows directly); random initial populations
+    scn = S.Scenario("Box", 19, 256, 9, 8, 0.6)
+    for f in ("z0", "zmax", "x0", "xmax", "y0", "ymax"):
+        scn.add_face(f, "noslip")
+    rng = np.random.default_rng(31 + steps)
+    scn.init = np.tile(scn.model.weights, (scn.ncells, 1)) * (1 + 0.05 * rng.standard_normal((scn.ncells, 19)))
+    with build_domain(scn, "fp64") as dom:
+        dom.step(steps)
+        pops = dom.populations()
+    want = oracle.run_port(scn, steps)["pops"]
+    mask = defined_entries(scn)
+    assert np.array_equal(pops[mask], want[mask])
+
+
+@pytest.mark.parametrize("q", [15, 27])
+def test_full_row_segments_other_stencils(q):
+    # the same with D3Q15 / D3Q27 in FP64 (bit for bit) and FP32 (against that FP64 run)
+    scn = S.Scenario("Box", q, 256, 7, 6, 0.7)
+    for f in ("z0", "zmax", "x0", "xmax", "y0", "ymax"):
+        scn.add_face(f, "noslip")
+    rng = np.random.default_rng(40 + q)
+    scn.init = np.tile(scn.model.weights, (scn.ncells, 1)) * (1 + 0.05 * rng.standard_normal((scn.ncells, q)))
+    mask = defined_entries(scn)
+    with build_domain(scn, "fp64") as dom:
+        dom.step(9)
+        p64 = dom.populations()
+    assert np.array_equal(p64[mask], oracle.run_port(scn, 9)["pops"][mask])
+    with build_domain(scn, "fp32") as dom:
+        dom.step(9)
+        p32 = dom.populations()
+    assert np.abs(p32[mask] - p64[mask]).max() < 1e-6
