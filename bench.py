@@ -46,6 +46,9 @@ def parse():
     ap.add_argument("--quick", action="store_true", help="headline only (no stencil sweep / e2e / cpu)")
     ap.add_argument("--extra-only", action="store_true",
                     help="only the Taylor-Green, 512^3 cavity and cavity-adjoint workloads")
+    ap.add_argument("--profile", choices=["fp64", "fp32", "fp16", "bf16"],
+                    help="only step the headline workload (warmup + steps) in this storage, no timing "
+                         "and no JSON line: the command the profiler runs")
     return ap.parse_args()
 
 
@@ -652,6 +655,14 @@ def main():
         line = run_reference(args, rank, world)
         if line is not None:
             print(json.dumps(line), flush=True)
+        return
+    if args.profile:
+        import torch
+        torch.cuda.set_device(local)
+        from lbm_gb300 import build_domain
+        with build_domain(workload(19, tuple(int(v) for v in args.size.split(","))), args.profile) as d:
+            d.step(args.warmup + args.steps)
+            d.sync()
         return
     if args.extra_only:
         import torch
