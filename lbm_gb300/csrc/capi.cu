@@ -16,6 +16,7 @@
 #include <new>
 #include <stdexcept>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "../../include/lbm_gb300.h"
@@ -337,11 +338,13 @@ void lbm_domain::build_side_lists()
     // earlier work on the stream may still read the lists released below
     check(cudaStreamSynchronize(stream), "side-list rebuild");
     std::vector<int> gxyz;
-    auto gf_lookup = [&](int x, int y, int z) -> int {
-        for (size_t j = 0; j < gxyz.size() / 3; ++j)
-            if (gxyz[3 * j] == x && gxyz[3 * j + 1] == y && gxyz[3 * j + 2] == z) return static_cast<int>(j);
-        gxyz.push_back(x); gxyz.push_back(y); gxyz.push_back(z);
-        return static_cast<int>(gxyz.size() / 3 - 1);
+    std::unordered_map<size_t, int> gf_index;  // layout index -> position in the ghost-fluid list
+    auto gf_add = [&](int x, int y, int z) -> int {
+        const auto it = gf_index.emplace(layout_index(x, y, z), static_cast<int>(gxyz.size() / 3));
+        if (it.second) {
+            gxyz.push_back(x); gxyz.push_back(y); gxyz.push_back(z);
+        }
+        return it.first->second;
     };
     auto is_fluid_h = [&](int x, int y, int z) {
         const uint8_t v = hm(x, y, z);
@@ -361,7 +364,7 @@ void lbm_domain::build_side_lists()
                     wrap(nx, ny, nz);
                     if (interior_fluid_h(nx, ny, nz)) adj = true;
                 }
-                if (adj) { gxyz.push_back(x); gxyz.push_back(y); gxyz.push_back(z); }
+                if (adj) gf_add(x, y, z);
             }
 
     // free-slip links (boundary.hpp:79-115)
@@ -397,7 +400,7 @@ void lbm_domain::build_side_lists()
                             l.w = static_cast<int>(layout_index(mx, my, mz));
                         } else {
                             l.y = q | (qs << 8) | (1 << 16);
-                            l.z = gf_lookup(sx, sy, sz);
+                            l.z = gf_add(sx, sy, sz);
                             l.w = 0;
                         }
                         links.push_back(l);
