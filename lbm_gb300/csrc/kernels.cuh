@@ -313,6 +313,41 @@ __device__ __forceinline__ void moments_shifted(const float (&s)[L::Q], float& d
     }
 }
 
+// The per-cell quantities of the shifted BGK relaxation, from the moments.
+struct ShiftedEq {
+    float ux, uy, uz, base, rA, rB;
+};
+__device__ __forceinline__ ShiftedEq shifted_eq(float drho, float jx, float jy, float jz)
+{
+    ShiftedEq e;
+    const float rho = 1.f + drho;
+    const float ir = __frcp_rn(rho);
+    e.ux = jx * ir, e.uy = jy * ir, e.uz = jz * ir;
+    e.base = fmaf(-rho * kC, e.ux * e.ux + e.uy * e.uy + e.uz * e.uz, drho);
+    e.rA = rho * kA, e.rB = rho * kB;
+    return e;
+}
+// The rest population relaxed.
+template <class L>
+__device__ __forceinline__ float relax_rest(const ShiftedEq& e, float omega, float s)
+{
+    return fmaf(omega, fmaf(static_cast<float>(L::w(L::REST)), e.base, -s), s);
+}
+// The pair (q, inv q) relaxed in one packed FP32x2 FMA chain: each lane performs the operations
+// fmaf(omega, fmaf(w, sym +- asym, -s), s) exactly as written for one population.
+template <class L>
+__device__ __forceinline__ float2 relax_pair(const ShiftedEq& e, int q, float omega, float sq, float sqb)
+{
+    const float cu = L::c(q, 0) * e.ux + L::c(q, 1) * e.uy + L::c(q, 2) * e.uz;
+    const float sym = fmaf(cu * cu, e.rB, e.base);
+    const float asym = cu * e.rA;
+    const float w = static_cast<float>(L::w(q));
+    const float2 ev = make_float2(sym + asym, sym - asym);
+    const float2 sv = make_float2(sq, sqb);
+    const float2 t = __ffma2_rn(make_float2(w, w), ev, make_float2(-sv.x, -sv.y));
+    return __ffma2_rn(make_float2(omega, omega), t, sv);
+}
+
 // BGK on shifted populations. Per opposite pair (q, inv q) the equilibria share
 // sym = drho - rho uu/(2 cs2) + rho cu^2/(2 cs4) and differ in the sign of asym = rho cu/cs2:
 //   s_eq,q - ... = w_q (sym +- asym),   s_q <- s_q + omega (w_q (sym +- asym) - s_q).
@@ -325,26 +360,13 @@ __device__ __forceinline__ void collide_shifted(float (&s)[L::Q], float omega, f
     m[1] = jx;
     m[2] = jy;
     m[3] = jz;
-    const float rho = 1.f + drho;
-    const float ir = __frcp_rn(rho);
-    const float ux = jx * ir, uy = jy * ir, uz = jz * ir;
-    const float base = fmaf(-rho * kC, ux * ux + uy * uy + uz * uz, drho);
-    const float rA = rho * kA, rB = rho * kB;
+    const ShiftedEq e = shifted_eq(drho, jx, jy, jz);
     constexpr int R = L::REST;
-    s[R] = fmaf(omega, fmaf(static_cast<float>(L::w(R)), base, -s[R]), s[R]);
+    s[R] = relax_rest<L>(e, omega, s[R]);
 #pragma unroll
     for (int q = 0; q < R; ++q) {
-        const float cu = L::c(q, 0) * ux + L::c(q, 1) * uy + L::c(q, 2) * uz;
-        const float sym = fmaf(cu * cu, rB, base);
-        const float asym = cu * rA;
-        const float w = static_cast<float>(L::w(q));
-        // the pair (q, inv q) in one packed FP32x2 FMA chain: each lane performs the operations
-        // fmaf(omega, fmaf(w, sym +- asym, -s), s) exactly as written for one population
         const int qb = L::Q - 1 - q;
-        const float2 e = make_float2(sym + asym, sym - asym);
-        const float2 sv = make_float2(s[q], s[qb]);
-        const float2 t = __ffma2_rn(make_float2(w, w), e, make_float2(-sv.x, -sv.y));
-        const float2 r = __ffma2_rn(make_float2(omega, omega), t, sv);
+        const float2 r = relax_pair<L>(e, q, omega, s[q], s[qb]);
         s[q] = r.x;
         s[qb] = r.y;
     }
