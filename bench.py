@@ -46,9 +46,11 @@ def parse():
     ap.add_argument("--quick", action="store_true", help="headline only (no stencil sweep / e2e / cpu)")
     ap.add_argument("--extra-only", action="store_true",
                     help="only the Taylor-Green, 512^3 cavity and cavity-adjoint workloads")
-    ap.add_argument("--profile", choices=["fp64", "fp32", "fp16", "bf16"],
-                    help="only step the headline workload (warmup + steps) in this storage, no timing "
-                         "and no JSON line: the command the profiler runs")
+    ap.add_argument("--profile", choices=["fp64", "fp32", "fp16", "bf16", "adjoint"],
+                    help="only step the headline workload (warmup + steps) in this storage, or run a "
+                         "gradient of the adjoint channel (128x64x64, FP32, warmup + steps forward steps, "
+                         "checkpoint every 10), with no timing and no JSON line: the command the "
+                         "profiler runs")
     return ap.parse_args()
 
 
@@ -660,6 +662,13 @@ def main():
         import torch
         torch.cuda.set_device(local)
         from lbm_gb300 import build_domain
+        from lbm_gb300 import scenario as S
+        if args.profile == "adjoint":
+            with build_domain(S.adjoint_channel(128, 64, 64, omega=1.7, seed=0), "fp32") as d:
+                d.adjoint_forward(args.warmup + args.steps, 10)
+                d.adjoint_backward((97, 128, 1, 64, 1, 64))
+                d.sync()
+            return
         with build_domain(workload(19, tuple(int(v) for v in args.size.split(","))), args.profile) as d:
             d.step(args.warmup + args.steps)
             d.sync()
