@@ -147,15 +147,24 @@ __device__ __forceinline__ void warp_flush_wall(double* grad_wall, int hid, cons
     }
 }
 
-// Blocks per SM the FP32 adjoint step is compiled for (0: no bound, FP64 is never bounded). 8 caps
-// it at 64 registers; D3Q27 then spills a few bytes in its handler path and the 256^3 cavity's
-// backward ran no faster (1.48 vs 1.47 ms per step), so the default leaves it unbounded.
-#ifndef LBMG_ADJ_MINB
-#define LBMG_ADJ_MINB 0
+// Blocks per SM the FP32 adjoint step is compiled for (0: no bound; FP64 is never bounded). The
+// kernel is latency-bound (on the 128x64x64 channel every pipe is below 11% busy with 20 of 64
+// warps active), so more resident warps pay where they cost no spills: D3Q15 and D3Q19 at 9 blocks
+// (56 registers; the channel's backward 52.2 against 56.0 us per step unbounded at 64). D3Q27
+// spills at 9 and stays unbounded (80 registers). LBMG_ADJ_MINB sets every stencil in tuning
+// builds.
+template <class L, class T>
+constexpr int adj_min_blocks()
+{
+#ifdef LBMG_ADJ_MINB
+    return sizeof(T) == 4 ? LBMG_ADJ_MINB : 0;
+#else
+    return sizeof(T) == 4 && L::Q != 27 ? 9 : 0;
 #endif
+}
 
 template <class L, class T>
-__global__ void __launch_bounds__(kBlockX, sizeof(T) == 4 ? LBMG_ADJ_MINB : 0) adjoint_step_kernel(const AdjParams<T> A)
+__global__ void __launch_bounds__(kBlockX, adj_min_blocks<L, T>()) adjoint_step_kernel(const AdjParams<T> A)
 {
     using K = AdjConst<T>;
     constexpr int Q = L::Q;
