@@ -314,7 +314,10 @@ def run_ours(args, rank, world, local):
         line["adjoint"] = {
             "channel128_fp32": {"bwd_over_fwd_per_step": adj["backward_over_forward"],
                                 "call_over_fwd": adj["backward_call_over_forward"],
-                                "fd_rel_err": adj["fd_check"]["max_rel_err_fp32_adjoint"]},
+                                "fd_rel_err": adj["fd_check"]["max_rel_err_fp32_adjoint"],
+                                "records_resident": {
+                                    "bwd_over_fwd_per_step": adj["records_resident"]["backward_over_forward"],
+                                    "call_over_fwd": adj["records_resident"]["backward_call_over_forward"]}},
             "cavity256_d3q27_fp16": {"bwd_over_fwd_per_step": cadj["backward_over_forward"],
                                      "call_over_fwd": cadj["backward_call_over_forward"],
                                      "fd_rel_err": cadj["fd_check"]["rel_err"]}}
@@ -338,8 +341,9 @@ def run_ours(args, rank, world, local):
 def run_adjoint(xl=128, yl=64, zl=64, steps=2000, ckpt=100):
     """Gradient workload: D3Q19 channel 128x64x64, per-cell inlet profile u_x ~ U[0.02, 0.05] and 5 %
     random solids from seed 0, omega 1.7, 2000 steps, checkpoints every 100 steps, objective = kinetic
-    energy in x in [96, 128) (interior cells 97..128). FP32 forward + adjoint; plain FP32 steps timed
-    beside it; the FP32 and FP64 adjoint gradients at three inlet cells against FP64 central finite
+    energy in x in [96, 128) (interior cells 97..128). FP32 forward + adjoint, with checkpoints and
+    recompute and with every step's record kept (ckpt_every = 1); plain FP32 steps timed beside it;
+    the FP32 and FP64 adjoint gradients at three inlet cells against FP64 central finite
     differences (h = 1e-5)."""
     from lbm_gb300 import build_domain
     from lbm_gb300 import scenario as S
@@ -348,6 +352,9 @@ def run_adjoint(xl=128, yl=64, zl=64, steps=2000, ckpt=100):
     with build_domain(scn, "fp32") as d:
         plain = time_steps(d, steps, 5)
     cost, (J32, (g32, _)) = _adjoint_costs(scn, "fp32", steps, ckpt, box)
+    # a checkpoint every step: the forward keeps every step's record (4 values per cell and step,
+    # 22 GB here) and the backward recomputes nothing
+    cost_res, (_, (g32_res, _)) = _adjoint_costs(scn, "fp32", steps, 1, box)
     with build_domain(scn, "fp64") as d:
         d.adjoint_forward(steps, ckpt)
         J64 = d.objective_ke(box)
@@ -376,6 +383,8 @@ def run_adjoint(xl=128, yl=64, zl=64, steps=2000, ckpt=100):
         "storage": "fp32 (f - w)", "steps": steps, "ckpt_every": ckpt,
         "forward_plain_ms_per_step": plain / steps * 1e3,
         **_adjoint_report(cost, plain / steps),
+        "records_resident": {**_adjoint_report(cost_res, plain / steps),
+                             "grad_rel_l2_vs_ckpt": _rel_l2(g32_res, g32)},
         "forward_mlups": n * steps / plain / 1e6,
         "J_fp32": J32, "J_fp64": J64,
         "fd_check": {"param": "inlet u_x at (y, z)", "cells": cells, "fd_fp64": fds,

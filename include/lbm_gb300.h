@@ -161,8 +161,11 @@ int lbm_reduce_mass_momentum(lbm_domain* d, double out[4]);
 
 /* Extension (no reference counterpart): gradients by a hand-written discrete adjoint of the step.
  * Forward: nsteps steps from the current state, keeping a copy of the state every ckpt_every
- * steps (device memory: ceil(nsteps / ckpt_every) copies of the population store). Not available
- * with free-slip cells or ghost cells without a handler (LBM_ERR_STATE). */
+ * steps (device memory: ceil(nsteps / ckpt_every) copies of the population store). ckpt_every = 1
+ * keeps no state copies: every step records each cell's mass and momentum instead (4 values per
+ * cell and step in the compute type, nsteps records; LBM_ERR_OOM if they do not fit), which is
+ * all the backward needs, so it then recomputes nothing. Not available with free-slip cells or
+ * ghost cells without a handler (LBM_ERR_STATE). */
 int lbm_adjoint_forward(lbm_domain* d, int64_t nsteps, int64_t ckpt_every);
 
 /* J = sum over the interior fluid cells of box = {x0, xE, y0, yE, z0, zE} (inclusive, interior
@@ -183,7 +186,8 @@ int lbm_adjoint_objective_ke(lbm_domain* d, const int64_t box[6], double* J);
  * Device memory (allocated by the first call and kept with the handle for the next ones, until a
  * geometry change, a run with another checkpoint interval, or lbm_destroy): two adjoint population
  * stores (Q values per cell in the compute type: FP32, or FP64 for FP64 storage), ckpt_every * 4
- * recorded values per cell, one copy of the population store and 3 doubles per cell. The
+ * recorded values per cell, one copy of the population store and 3 doubles per cell (after a
+ * ckpt_every = 1 forward: the adjoint stores and the gradients only, beside its records). The
  * gradients are scaled by dJ on the device and copied into the caller's arrays. Synchronises. */
 int lbm_adjoint_backward(lbm_domain* d, const int64_t box[6], double dJ, double* grad_inflow,
                          double* grad_wall);

@@ -151,7 +151,7 @@ __device__ __forceinline__ void warp_flush_wall(double* grad_wall, int hid, cons
 // kernel is latency-bound (on the 128x64x64 channel every pipe is below 11% busy with 20 of 64
 // warps active), so more resident warps pay where they cost no spills: D3Q15 and D3Q19 at 9 blocks
 // (56 registers; the channel's backward 52.2 against 56.0 us per step unbounded at 64). D3Q27
-// spills at 9 and stays unbounded (80 registers). LBMG_ADJ_MINB sets every stencil in tuning
+// spills at 9 and stays unbounded (68 registers). LBMG_ADJ_MINB sets every stencil in tuning
 // builds.
 template <class L, class T>
 constexpr int adj_min_blocks()

@@ -119,15 +119,19 @@ struct DevBuf {
 
 // Checkpoints of a gradient run (lbm_adjoint_forward .. lbm_adjoint_backward), and the backward's
 // workspace: allocated by the first lbm_adjoint_backward of a run's geometry and checkpoint
-// interval and kept for the next calls, so that repeated gradients cost no allocation.
+// interval and kept for the next calls, so that repeated gradients cost no allocation. A run with
+// a checkpoint every step (k = 1) keeps the forward's per-step records instead of state copies:
+// the backward then recomputes nothing and leaves the state alone.
 struct AdjointRun {
     bool ready = false;
+    bool resident = false;  // k = 1: rec holds the records of all n steps, written by the forward
     long long s0 = 0;  // steps done when the run started
     long long n = 0;   // steps of the run
     long long k = 0;   // steps between checkpoints
     std::vector<std::unique_ptr<DevBuf<unsigned char>>> ckpt;  // state after s0 + j*k steps
     DevBuf<unsigned char> mu[2];   // adjoint populations mu_t, mu_{t-1}
-    DevBuf<unsigned char> rec;     // the recorded mass and momentum of a segment's k steps
+    DevBuf<unsigned char> rec;     // the recorded mass and momentum of a segment's k steps (of
+                                   // all n steps when resident)
     DevBuf<unsigned char> backup;  // the state the forward run left
     DevBuf<double> gin, gwall;     // gradients (inflow cells, wall handlers)
     void release_workspace()
@@ -167,6 +171,7 @@ struct lbm_domain {
     DevBuf<uint2> link;     // per-cell link words and LinkRecord rows
     DevBuf<int> edge;       // kFluidEdge cells
     DevBuf<LinkRecord> ltab;  // LinkRecords (shifted storage)
+    DevBuf<uint8_t> wmask;    // the step kernel's per-segment warp mask
     DevBuf<int> errword;    // device error word, a list counter
     DevBuf<double> mon;     // step monitor accumulators
     DevBuf<double> mon_ring;  // per-step monitor results, kMonRing slots of 4 doubles
@@ -451,6 +456,10 @@ void lbm_domain::finalize()
     check(cudaMemcpyAsync(bc.p, bcs.data(), bcs.size() * sizeof(BcEntry), cudaMemcpyHostToDevice, stream),
           "upload handler table");
     ops->classify(dev, stream);  // reads the handler table (no-slip links)
+    const size_t nseg = row_segments(g, ops->row_cells);
+    if (wmask.n != nseg) wmask.alloc(nseg, "cudaMalloc(warp mask)");
+    ops->warp_mask(dev, wmask.p, stream);
+    dev.wmask = wmask.p;
     // merged inflow profile in reference cell order
     bool any_profile = false;
     for (const auto& p : profiles) any_profile = any_profile || !p.empty();
@@ -1027,7 +1036,7 @@ int lbm_memory_info(const lbm_domain* d, uint64_t* device_bytes, uint64_t* step_
             *device_bytes = m->pop.bytes() + m->flag.bytes() + m->bc.bytes() + m->profile.bytes() + m->gf_xyz.bytes() +
                             m->gf_pop.bytes() + m->fs_link.bytes() + m->red.bytes() + m->link.bytes() + m->edge.bytes() +
                             m->errword.bytes() + m->mon.bytes() + m->mon_ring.bytes() + m->stage.bytes() + m->ltab.bytes() +
-                            m->adj.mu[0].bytes() + m->adj.mu[1].bytes() + m->adj.rec.bytes() + m->adj.backup.bytes() +
+                            m->wmask.bytes() + m->adj.mu[0].bytes() + m->adj.mu[1].bytes() + m->adj.rec.bytes() + m->adj.backup.bytes() +
                             m->adj.gin.bytes() + m->adj.gwall.bytes();
         if (device_bytes)
             for (const auto& c : m->adj.ckpt) *device_bytes += c->bytes();
@@ -1066,6 +1075,23 @@ int lbm_adjoint_forward(lbm_domain* d, int64_t nsteps, int64_t ckpt_every)
         a.s0 = d->steps;
         a.n = nsteps;
         a.k = ckpt_every;
+        a.resident = ckpt_every == 1;
+        // a record buffer of another size (a previous run's) goes before this run allocates
+        const size_t rec_bytes = 4 * d->dev.g.PS * d->ops->compute_bytes;
+        const size_t rec_need = static_cast<size_t>(a.resident ? nsteps : ckpt_every) * rec_bytes;
+        if (a.rec.bytes() != rec_need) a.rec.release();
+        if (a.resident) {
+            // every step records its cell moments (what the backward's recompute would record)
+            a.backup.release();
+            if (!a.rec.p) a.rec.alloc(rec_need, "cudaMalloc(step records)");
+            for (long long r = 0; r < nsteps; ++r)
+                d->ops->step(d->dev, d->steps + 1 + r, -1, nullptr, a.rec.p + r * rec_bytes, d->stream);
+            d->steps += nsteps;
+            check(cudaGetLastError(), "step kernel launch");
+            d->state_custom = true;
+            a.ready = true;
+            return;
+        }
         const long long nseg = (nsteps + ckpt_every - 1) / ckpt_every;
         for (long long j = 0; j < nseg; ++j) {
             a.ckpt.emplace_back(new DevBuf<unsigned char>());
@@ -1117,31 +1143,41 @@ int lbm_adjoint_backward(lbm_domain* d, const int64_t box[6], double dJ, double*
         auto& gin = a.gin;
         auto& gwall = a.gwall;
         const size_t mu_bytes = static_cast<size_t>(d->Q) * PS * Tb;
-        if (mu[0].bytes() != mu_bytes || rec.bytes() != static_cast<size_t>(a.k) * rec_bytes) {
-            a.release_workspace();
+        if (mu[0].bytes() != mu_bytes) {
             mu[0].alloc(mu_bytes, "cudaMalloc(adjoint populations)");
             mu[1].alloc(mu_bytes, "cudaMalloc(adjoint populations)");
-            rec.alloc(static_cast<size_t>(a.k) * rec_bytes, "cudaMalloc(recompute record)");
-            backup.alloc(d->pop.bytes(), "cudaMalloc(state backup)");
             gin.alloc(3 * d->ng, "cudaMalloc(inflow gradient)");
             gwall.alloc(3 * kMaxHandlers, "cudaMalloc(wall gradient)");
+        }
+        if (a.resident) {
+            backup.release();  // no recompute: the state is never touched
+        } else {
+            if (rec.bytes() != static_cast<size_t>(a.k) * rec_bytes)
+                rec.alloc(static_cast<size_t>(a.k) * rec_bytes, "cudaMalloc(recompute record)");
+            if (backup.bytes() != d->pop.bytes()) backup.alloc(d->pop.bytes(), "cudaMalloc(state backup)");
         }
         check(cudaMemsetAsync(gin.p, 0, gin.bytes(), d->stream), "clear gradient");
         check(cudaMemsetAsync(gwall.p, 0, gwall.bytes(), d->stream), "clear gradient");
         check(cudaMemsetAsync(mu[0].p, 0, mu[0].bytes(), d->stream), "clear adjoint");
         check(cudaMemsetAsync(mu[1].p, 0, mu[1].bytes(), d->stream), "clear adjoint");
-        check(cudaMemcpyAsync(backup.p, d->pop.p, d->pop.bytes(), cudaMemcpyDeviceToDevice, d->stream), "state backup");
+        if (!a.resident)
+            check(cudaMemcpyAsync(backup.p, d->pop.p, d->pop.bytes(), cudaMemcpyDeviceToDevice, d->stream),
+                  "state backup");
 
-        const long long nseg = static_cast<long long>(a.ckpt.size());
+        // resident: one segment of all n steps whose records the forward wrote
+        const long long nseg = a.resident ? 1 : static_cast<long long>(a.ckpt.size());
+        const long long seg_len = a.resident ? a.n : a.k;
         int cur = 0;
         long long t_cur = 0;  // mu[cur] holds mu_{t_cur}
         for (long long j = nseg - 1; j >= 0; --j) {
-            const long long c = a.s0 + j * a.k;
-            const long long len = std::min<long long>(a.k, a.n - j * a.k);
-            check(cudaMemcpyAsync(d->pop.p, a.ckpt[j]->p, d->pop.bytes(), cudaMemcpyDeviceToDevice, d->stream),
-                  "restore checkpoint");
-            for (long long r = 1; r <= len; ++r)  // recompute, recording rec_{c+r}
-                d->ops->step(d->dev, c + r, -1, nullptr, rec.p + (r - 1) * rec_bytes, d->stream);
+            const long long c = a.s0 + j * seg_len;
+            const long long len = std::min<long long>(seg_len, a.n - j * seg_len);
+            if (!a.resident) {
+                check(cudaMemcpyAsync(d->pop.p, a.ckpt[j]->p, d->pop.bytes(), cudaMemcpyDeviceToDevice, d->stream),
+                      "restore checkpoint");
+                for (long long r = 1; r <= len; ++r)  // recompute, recording rec_{c+r}
+                    d->ops->step(d->dev, c + r, -1, nullptr, rec.p + (r - 1) * rec_bytes, d->stream);
+            }
             if (j == nseg - 1) {
                 d->ops->adj_terminal(d->dev, rec.p + (len - 1) * rec_bytes, mu[cur].p, b, d->stream);
                 t_cur = c + len;
@@ -1155,7 +1191,9 @@ int lbm_adjoint_backward(lbm_domain* d, const int64_t box[6], double dJ, double*
                 t_cur = t - 1;
             }
         }
-        check(cudaMemcpyAsync(d->pop.p, backup.p, d->pop.bytes(), cudaMemcpyDeviceToDevice, d->stream), "restore state");
+        if (!a.resident)
+            check(cudaMemcpyAsync(d->pop.p, backup.p, d->pop.bytes(), cudaMemcpyDeviceToDevice, d->stream),
+                  "restore state");
         // times the upstream gradient on the device, then straight into the caller's arrays
         scale_doubles(gin.p, gin.n, dJ, d->stream);
         scale_doubles(gwall.p, gwall.n, dJ, d->stream);

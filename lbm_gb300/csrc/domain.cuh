@@ -142,6 +142,9 @@ struct DomainDev {
     const int* edge;
     int n_edge;
     const LinkRecord* ltab;  // rows named by link[i].y
+    // One byte per row segment of the step kernel: bit w = the segment's warp w holds only
+    // kFluidBulk cells (see warp_mask_kernel).
+    const uint8_t* wmask;
     // Device error word: set to 1 by a kernel whose bounded wait gave up.
     int* err;
     // Step monitor accumulators: two sets of kMonBuckets x 4 doubles, used by alternate monitored

@@ -299,17 +299,22 @@ __device__ __forceinline__ float seq_shifted(int q, float drho, float rho, float
     return static_cast<float>(rt_w<L>(q)) * (drho + rho * (cu * (kA + cu * kB) - uu_c));
 }
 
+// Mass and momentum over opposite pairs: the sum s_q + s_inv(q) enters the mass, the difference
+// s_q - s_inv(q) each momentum component where c_q has one (one subtraction per pair instead of
+// one per direction and component).
 template <class L>
 __device__ __forceinline__ void moments_shifted(const float (&s)[L::Q], float& drho, float& jx,
                                                 float& jy, float& jz)
 {
-    drho = 0.f; jx = 0.f; jy = 0.f; jz = 0.f;
+    drho = s[L::REST]; jx = 0.f; jy = 0.f; jz = 0.f;
 #pragma unroll
-    for (int q = 0; q < L::Q; ++q) {
-        drho += s[q];
-        if (L::c(q, 0) > 0) jx += s[q]; else if (L::c(q, 0) < 0) jx -= s[q];
-        if (L::c(q, 1) > 0) jy += s[q]; else if (L::c(q, 1) < 0) jy -= s[q];
-        if (L::c(q, 2) > 0) jz += s[q]; else if (L::c(q, 2) < 0) jz -= s[q];
+    for (int q = 0; q < L::REST; ++q) {
+        const int qb = L::Q - 1 - q;
+        const float sum = s[q] + s[qb], dif = s[q] - s[qb];
+        drho += sum;
+        if (L::c(q, 0) > 0) jx += dif; else if (L::c(q, 0) < 0) jx -= dif;
+        if (L::c(q, 1) > 0) jy += dif; else if (L::c(q, 1) < 0) jy -= dif;
+        if (L::c(q, 2) > 0) jz += dif; else if (L::c(q, 2) < 0) jz -= dif;
     }
 }
 
@@ -321,7 +326,10 @@ __device__ __forceinline__ ShiftedEq shifted_eq(float drho, float jx, float jy, 
 {
     ShiftedEq e;
     const float rho = 1.f + drho;
-    const float ir = __frcp_rn(rho);
+    // the hardware reciprocal (rcp.approx: at most 1 ulp from 1/rho, rho near 1): the velocity
+    // keeps FP32 rounding level, for one instruction instead of a correctly rounded sequence
+    float ir;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(ir) : "f"(rho));
     e.ux = jx * ir, e.uy = jy * ir, e.uz = jz * ir;
     e.base = fmaf(-rho * kC, e.ux * e.ux + e.uy * e.uy + e.uz * e.uz, drho);
     e.rA = rho * kA, e.rB = rho * kB;
@@ -426,6 +434,7 @@ struct StepParams {
     const int* edge;       // layout indices of the kFluidEdge cells, increasing
     int n_edge;
     const LinkRecord* ltab;
+    const uint8_t* wmask;  // per row segment: bit w = warp w covers kFluidBulk cells only
     int* err;              // set to 1 when a bounded wait gives up
     double* mon;           // kMonBuckets x 4 FP64 accumulators of the step's mass and momentum,
                            // or nullptr
@@ -624,12 +633,26 @@ constexpr size_t link_smem_bytes()
 {
     return Store<S>::kShifted ? static_cast<size_t>(kLinkWords) * kRowCells * 4 : 0;
 }
-// Dynamic shared memory of a step-kernel block: a row block's stages and then its LinkRecords, or
-// an edge block's scratch from the start, whichever is larger.
+// Warps with at most this many kFluidWall cells take the shared handler path (link_values_warp);
+// the others (a row along a wall, every lane with links) the per-lane one.
+#ifndef LBMG_WARP_LINK_CELLS
+#define LBMG_WARP_LINK_CELLS 4
+#endif
+constexpr int kWarpLinkCells = LBMG_WARP_LINK_CELLS;
+
+// The warp scratch of the shared handler path (link_values_warp): per warp, the Q post-collision
+// populations and the 4 moments of each of up to kWarpLinkCells cells.
+template <class L, class S>
+constexpr size_t warp_scratch_bytes()
+{
+    return static_cast<size_t>(kRowCells / 32) * kWarpLinkCells * (L::Q + 4) * sizeof(typename Store<S>::C);
+}
+// Dynamic shared memory of a step-kernel block: a row block's stages, its LinkRecords and the warp
+// scratch, or an edge block's scratch from the start, whichever is larger.
 template <class L, class S>
 constexpr size_t row_smem_bytes()
 {
-    const size_t rows = segs<S>() * stage_bytes<L, S>() + link_smem_bytes<S>();
+    const size_t rows = segs<S>() * stage_bytes<L, S>() + link_smem_bytes<S>() + warp_scratch_bytes<L, S>();
     const size_t edge = edge_scratch_bytes<L, S>();
     return rows > edge ? rows : edge;
 }
@@ -811,6 +834,75 @@ __device__ __forceinline__ void link_values(const StepParams<S>& P, int i, typen
     }
 }
 
+// Handler values (as link_values) of the kFluidWall cells of a warp that holds only a few of them,
+// typically the one cell next to an inlet or outlet at the end of a row, whose per-lane path would
+// hold the other 31 lanes for its whole length. Each such cell (a source lane, the k-th lane of
+// `need`) has put its post-collision populations and moments into slot k of the warp's scratch
+// (warp_link_source); here, per source, lane ip stores the value of link ip. Every lane of the warp
+// calls it with the same `need` (at most kWarpLinkCells lanes with links); wl is 0 on the other
+// lanes. Same operations per value as link_values.
+template <class L, class S, bool ODD>
+__device__ __forceinline__ void link_values_warp(S* pop, unsigned need, int i, uint32_t wl, int has_rec,
+                                              const uint32_t* rec_warp, const typename Store<S>::C* scr,
+                                              size_t ps, int sy, int sz)
+{
+    using St = Store<S>;
+    using T = typename St::C;
+    constexpr int Q = L::Q;
+    constexpr int SW = Q + 4;  // scratch words of one source
+    constexpr unsigned kFull = 0xffffffffu;
+    const int ip = static_cast<int>(threadIdx.x & 31u);  // this lane's link
+    for (unsigned rem = need; rem; rem &= rem - 1u, scr += SW) {
+        const int src = __ffs(rem) - 1;
+        const uint32_t swl = __shfl_sync(kFull, wl, src);
+        const int si = __shfl_sync(kFull, i, src);
+        const int srec = __shfl_sync(kFull, has_rec, src);
+        if (ip < Q && ((swl >> ip) & 1u)) {
+            // direction p = inv(ip): after an odd step slot ip at the source cell x, after an even
+            // step plane p at x + c_p
+            const int p = Q - 1 - ip;
+            const int cx = rt_c<L>(p, 0), cy = rt_c<L>(p, 1), cz = rt_c<L>(p, 2);
+            T v = scr[p];
+            if constexpr (St::kShifted) {
+                const uint32_t* r = rec_warp + kLinkWords * src;
+                if (srec && ((r[0] >> ip) & 1u)) {
+                    const uint32_t wallm = r[1], valm = wallm | r[2];
+                    if ((valm >> ip) & 1u) {
+                        const int k = min(__popc(valm & ((1u << ip) - 1u)), kMaxRecordValues - 1);
+                        const float c = __uint_as_float(r[5 + k]);
+                        v = ((wallm >> ip) & 1u) ? fmaf(c, 1.f + scr[Q], v) : c;
+                    } else {
+                        const float r0 = __uint_as_float(r[3]), ir0 = __uint_as_float(r[4]);
+                        const float ux = scr[Q + 1] * ir0, uy = scr[Q + 2] * ir0, uz = scr[Q + 3] * ir0;
+                        const float uu_c = (ux * ux + uy * uy + uz * uz) * kC;
+                        const float cu = static_cast<float>(cx) * ux + static_cast<float>(cy) * uy +
+                                         static_cast<float>(cz) * uz;
+                        v = 2.f * static_cast<float>(rt_w<L>(p)) * ((r0 - 1.f) + r0 * fmaf(cu * cu, kB, -uu_c)) - v;
+                    }
+                }
+            }
+            const long long off = ODD ? static_cast<long long>(ip) * static_cast<long long>(ps)
+                                      : static_cast<long long>(p) * static_cast<long long>(ps) +
+                                            (cx + cy * sy + cz * sz);
+            St::st(pop + si + off, v);
+        }
+    }
+}
+
+// A source lane of link_values_warp: its populations and moments into its slot of the scratch.
+template <class L, class S>
+__device__ __forceinline__ void warp_link_source(unsigned need, const typename Store<S>::C (&f)[L::Q],
+                                                 const typename Store<S>::C (&m)[4], typename Store<S>::C* scr)
+{
+    constexpr int Q = L::Q;
+    const unsigned lane = threadIdx.x & 31u;
+    typename Store<S>::C* mine = scr + (Q + 4) * __popc(need & ((1u << lane) - 1u));
+#pragma unroll
+    for (int q = 0; q < Q; ++q) mine[q] = f[q];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) mine[Q + k] = m[k];
+}
+
 // The Q bulk stores of a row-block cell at layout pointer `cell`, plane by plane through one
 // running pointer (each step adds a block-uniform delta: the plane stride and, on odd steps, the
 // change of the shift c_p).
@@ -909,12 +1001,17 @@ __device__ __forceinline__ void row_block(const StepParams<S>& P, int rb, int ns
         // links of a kFluidWall cell (bit q: x - c_q is a no-slip, moving-wall, inflow, outflow
         // or pressure cell), and its LinkRecord, copied into shared memory while the rows are in
         // flight (shifted storage). Cells on a face of the domain, where boundaries usually sit,
-        // load their link word together with their flag instead of after it.
-        const bool face = x == 1 || x == P.g.xl || y == 1 || y == P.g.yl || z == 1 || z == P.g.zl;
-        const uint2 lkf = face && x <= P.g.xl ? P.link[i] : make_uint2(0u, kNoRecord);
-        const uint8_t fl = x <= P.g.xl ? P.flag[i] : static_cast<uint8_t>(kFluidEdge);
-        bool bulk = fl == kFluidBulk || fl == kFluidWall;
-        const uint2 lk = fl != kFluidWall ? make_uint2(0u, kNoRecord) : face ? lkf : P.link[i];
+        // load their link word together with their flag instead of after it. A warp whose cells
+        // are all kFluidBulk (the segment's warp mask) loads neither.
+        bool bulk = true;
+        uint2 lk = make_uint2(0u, kNoRecord);
+        if (!((P.wmask[seg0 + s] >> (tx >> 5)) & 1u)) {
+            const bool face = x == 1 || x == P.g.xl || y == 1 || y == P.g.yl || z == 1 || z == P.g.zl;
+            const uint2 lkf = face && x <= P.g.xl ? P.link[i] : make_uint2(0u, kNoRecord);
+            const uint8_t fl = x <= P.g.xl ? P.flag[i] : static_cast<uint8_t>(kFluidEdge);
+            bulk = fl == kFluidBulk || fl == kFluidWall;
+            lk = fl != kFluidWall ? make_uint2(0u, kNoRecord) : face ? lkf : P.link[i];
+        }
         const uint32_t wl = lk.x;
         uint32_t* rec = nullptr;
         if constexpr (St::kShifted) {
@@ -934,19 +1031,13 @@ __device__ __forceinline__ void row_block(const StepParams<S>& P, int rb, int ns
             bulk = false;
         }
         T m[4] = {T(0), T(0), T(0), T(0)};
+        T f[Q];
         if (bulk) {
             const S* buf = reinterpret_cast<const S*>(smem_raw + s * SB);
-            T f[Q];
 #pragma unroll
             for (int q = 0; q < Q; ++q) f[q] = St::ld(buf + q * W + PAD + tx - (ODD ? L::c(q, 0) : 0));
             collide_any<L, S>(f, P, m);
             if (INSTR && P.rec) record_moments<S>(P.rec, i, m);
-            if (wl) {
-                if constexpr (St::kShifted) {
-                    if (rec) cp_async_wait_all();
-                }
-                link_values<L, S, ODD>(P, i, f, m, wl, rec, opaque(PS), opaque(sy));
-            }
             // stores plane by plane through one running pointer: each step adds a block-uniform
             // delta (the plane stride, and on odd steps the change of the shift c_p). Streaming
             // (evict-first) stores when every cell is a row-block cell (see l2_stream_policy).
@@ -957,6 +1048,32 @@ __device__ __forceinline__ void row_block(const StepParams<S>& P, int rb, int ns
         } else if constexpr (St::kShifted) {
             if (rec) cp_async_wait_all();  // no copy may still be landing when the block ends
         }
+        // handler values, into slots that no cell's own stores touch: shared by the warp when
+        // few of its cells have links, else per lane
+        const uint32_t wlb = bulk ? wl : 0u;
+        const unsigned need = __ballot_sync(0xffffffffu, wlb != 0u);
+        if (need) {
+            if (__popc(need) <= kWarpLinkCells) {
+                const uint32_t* rec_warp =
+                    reinterpret_cast<const uint32_t*>(smem_raw + kSegs * SB) + kLinkWords * (tx & ~31);
+                T* scr = reinterpret_cast<T*>(smem_raw + kSegs * SB + link_smem_bytes<S>()) +
+                         (tx >> 5) * kWarpLinkCells * (Q + 4);
+                if (wlb) {
+                    if constexpr (St::kShifted) {
+                        if (rec) cp_async_wait_all();  // this lane's LinkRecord has landed
+                    }
+                    warp_link_source<L, S>(need, f, m, scr);
+                }
+                __syncwarp();
+                link_values_warp<L, S, ODD>(pop, need, i, wlb, rec != nullptr, rec_warp, scr, PS, sy, sz);
+                __syncwarp();  // the scratch is read before the warp's next segment writes it
+            } else if (wlb) {
+                if constexpr (St::kShifted) {
+                    if (rec) cp_async_wait_all();
+                }
+                link_values<L, S, ODD>(P, i, f, m, wlb, rec, opaque(PS), opaque(sy));
+            }
+        }
         if constexpr (INSTR) {
 #pragma unroll
             for (int k = 0; k < 4; ++k) macc[k] += m[k];
@@ -966,19 +1083,14 @@ __device__ __forceinline__ void row_block(const StepParams<S>& P, int rb, int ns
 }
 
 // Resident blocks per SM that the register allocation of a step kernel must allow (0: no
-// bound; ptxas then picks fewer registers than with an explicit 1). Unbounded, the shifted
-// D3Q19 kernels take 56 registers (9 blocks per SM); bounded to 10 blocks they keep 48. The
-// D3Q15 ones run at 12 blocks per SM (40 registers): 46.7k against 43.9k MLUPS at 10 blocks on
-// the 256x128x128 channel in FP32. D3Q27 gains nothing from a bound (6, 7 and 8 blocks: 20.9k,
-// 23.1k, 23.3k against 23.4k unbounded); FP64 is never bounded. LBMG_MINB_Q15 / LBMG_MINB_Q27 set the D3Q15 and
-// D3Q27 values in tuning builds. LBMG_MINB_EVEN / LBMG_MINB_ODD override the shifted-storage
-// values in tuning builds.
-#ifndef LBMG_MINB_Q15
-#define LBMG_MINB_Q15 12
-#endif
-#ifndef LBMG_MINB_Q27
-#define LBMG_MINB_Q27 0
-#endif
+// bound; ptxas then picks fewer registers than with an explicit 1). Shifted D3Q19 kernels: 10
+// blocks (48 registers; unbounded they take 56, 9 blocks). D3Q15: 12 blocks (40 registers) for
+// FP32 (46.5k against 45.4k MLUPS at 10 on the 256x128x128 channel), 10 for 16-bit storage (67.3k
+// against 65.3k at 12, where the 40-register kernels spill). D3Q27: unbounded for FP32 (72-80
+// registers; 23.7k against 23.5k at 8) and 8 blocks for 16-bit storage (64 registers; 40.3k
+// against 38.7k unbounded). FP64 is never bounded. LBMG_MINB_Q15 / LBMG_MINB_Q27 set the D3Q15
+// and D3Q27 values of every storage type, LBMG_MINB_EVEN / LBMG_MINB_ODD the shifted-storage
+// values, in tuning builds.
 template <class L, class S, bool ODD, bool INSTR>
 constexpr int min_blocks()
 {
@@ -995,7 +1107,16 @@ constexpr int min_blocks()
         // bounds: D3Q15 at 40 registers, D3Q19 at 48
         if (INSTR && L::Q == 15) return 10;
         if (INSTR && L::Q == 19) return 9;
-        return L::Q == 19 ? 10 : L::Q == 27 ? LBMG_MINB_Q27 : LBMG_MINB_Q15;
+        constexpr bool k16 = sizeof(S) == 2;
+        if (L::Q == 19) return 10;
+#ifdef LBMG_MINB_Q15
+        if (L::Q == 15) return LBMG_MINB_Q15;
+#endif
+#ifdef LBMG_MINB_Q27
+        if (L::Q == 27) return LBMG_MINB_Q27;
+#endif
+        if (L::Q == 15) return k16 ? 10 : 12;
+        return k16 ? 8 : 0;
     }
 }
 

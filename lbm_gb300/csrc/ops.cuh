@@ -52,7 +52,18 @@ struct KernelOps {
     // kinetic energy of the box into out[0] (device), partials as for reduce
     void (*objective_ke)(const DomainDev& d, long long k, Box box, double* partials, int reduce_blocks,
                          double* out, cudaStream_t s);
+    // the step kernel's per-segment warp mask (d.flag classified) into out, one byte per segment
+    // (row_segments(d.g, row_cells))
+    void (*warp_mask)(const DomainDev& d, uint8_t* out, cudaStream_t s);
+    // cells per row segment of the step kernel
+    int row_cells;
 };
+
+// Row segments of the step kernel: ceil(xl / row_cells) per row, rows in (y, z) order.
+inline size_t row_segments(const Geom& g, int row_cells)
+{
+    return static_cast<size_t>((g.xl + row_cells - 1) / row_cells) * g.yl * g.zl;
+}
 
 const KernelOps* ops_fp64(int q);
 const KernelOps* ops_fp32(int q);

@@ -40,6 +40,7 @@ StepParams<S> step_params(const DomainDev& d)
     p.edge = d.edge;
     p.n_edge = d.n_edge;
     p.ltab = d.ltab;
+    p.wmask = d.wmask;
     p.profile = d.profile;
     p.g = d.g;
     p.err = d.err;
@@ -256,12 +257,21 @@ struct Launch {
                                                                  capacity);
     }
 
+    static void warp_mask(const DomainDev& d, uint8_t* out, cudaStream_t s)
+    {
+        const int nseg_x = (d.g.xl + kRowCells - 1) / kRowCells;
+        warp_mask_kernel<<<dim3(static_cast<unsigned>(nseg_x), static_cast<unsigned>(d.g.yl),
+                                static_cast<unsigned>(d.g.zl)),
+                           kRowCells, 0, s>>>(d.flag, d.g, nseg_x, out);
+    }
+
     static const KernelOps* table()
     {
         static const KernelOps t = {&init,         &classify,      &step,          &monitor_fold, &gather,
                                     &scatter,      &moments,       &gather_range,  &scatter_range,
                                     &moments_range, &ghost_fluid_slots, &reduce,   sizeof(T),
-                                    &adj_terminal, &adj_step,      &link_table,    &objective_ke};
+                                    &adj_terminal, &adj_step,      &link_table,    &objective_ke,
+                                    &warp_mask,    kRowCells};
         return &t;
     }
 };

@@ -25,8 +25,8 @@ __global__ void init_kernel(S* pop, size_t PS)
 // The lattice is symmetric, so the pull neighbours x - c_q are also all the push neighbours.
 template <class L>
 // special_ok (shifted storage): links to moving-wall, inflow, outflow and pressure cells (at most
-// at most kMaxRecordValues moving-wall and inflow links, one outlet density) keep a cell in the
-// row blocks, served by its LinkRecord.
+// kMaxRecordValues moving-wall and inflow links, one outlet density) keep a cell in the row blocks,
+// served by its LinkRecord.
 __global__ void classify_kernel(uint8_t* flag, uint2* link, const BcEntry* bc, Geom g, bool special_ok)
 {
     const int x = 1 + static_cast<int>(blockIdx.x) * kBlockX + static_cast<int>(threadIdx.x);
@@ -65,6 +65,27 @@ __global__ void classify_kernel(uint8_t* flag, uint2* link, const BcEntry* bc, G
     if (values > kMaxRecordValues) edge = true;
     flag[i] = edge ? kFluidEdge : (m ? kFluidWall : kFluidBulk);
     link[i] = make_uint2(m, kNoRecord);
+}
+
+// Per row segment of the step kernel (kRowCells cells of one row from x0; segment index
+// sx + nseg_x * ((y - 1) + yl * (z - 1)), the row blocks' order): bit w set when the segment's warp
+// w covers kFluidBulk cells only, all inside the row. Row blocks skip the per-cell flag, link and
+// handler work of such a warp. Grid (nseg_x, yl, zl), kRowCells threads.
+static __global__ void __launch_bounds__(kRowCells) warp_mask_kernel(const uint8_t* flag, Geom g, int nseg_x,
+                                                                     uint8_t* wmask)
+{
+    __shared__ unsigned bits;
+    if (threadIdx.x == 0) bits = 0u;
+    __syncthreads();
+    const int sx = static_cast<int>(blockIdx.x);
+    const int y = 1 + static_cast<int>(blockIdx.y), z = 1 + static_cast<int>(blockIdx.z);
+    const int x = 1 + sx * kRowCells + static_cast<int>(threadIdx.x);
+    const bool bulk = x <= g.xl && flag[cidx(g, x, y, z)] == kFluidBulk;
+    if (__all_sync(0xffffffffu, bulk) && (threadIdx.x & 31u) == 0u) atomicOr(&bits, 1u << (threadIdx.x >> 5));
+    __syncthreads();
+    if (threadIdx.x == 0)
+        wmask[sx + static_cast<size_t>(nseg_x) * ((y - 1) + static_cast<size_t>(g.yl) * (z - 1))] =
+            static_cast<uint8_t>(bits);
 }
 
 // LinkRecord of every kFluidWall cell with links to handlers other than no-slip (shifted

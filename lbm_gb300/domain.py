@@ -287,7 +287,8 @@ class Domain:
 
     # -- gradients (extension) -------------------------------------------------------------
     def adjoint_forward(self, nsteps: int, ckpt_every: int) -> None:
-        """nsteps steps from the current state, checkpointing every ckpt_every steps."""
+        """nsteps steps from the current state, checkpointing every ckpt_every steps (1: every step's
+        cell mass and momentum kept instead of state copies; the backward then recomputes nothing)."""
         check(self._lib.lbm_adjoint_forward(self._h, int(nsteps), int(ckpt_every)), self._h)
 
     def objective_ke(self, box) -> float:

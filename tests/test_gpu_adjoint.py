@@ -228,6 +228,46 @@ def test_backward_restores_state_and_can_repeat():
         assert d.steps_done == 30
 
 
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_resident_records_match_recompute(precision):
+    # ckpt_every = 1 keeps every step's record from the forward: no recompute, the state is never
+    # touched. Two handles in lockstep run the same forward steps with the two kinds of run in
+    # turn, so each stage compares both on the same starting state (and the handle's workspace is
+    # reallocated between the kinds). The adjoint is the same arithmetic on the same records; only
+    # the order of the FP64 gradient atomics differs.
+    scn = _channel()
+    with build_domain(scn, precision) as a, build_domain(scn, precision) as b:
+        for ka, kb in ((1, 13), (13, 1), (1, 7)):
+            a.adjoint_forward(60, ka)
+            b.adjoint_forward(60, kb)
+            before = a.populations()
+            assert np.array_equal(before, b.populations())
+            ga, gwa = a.adjoint_backward(CH_BOX)
+            gb, gwb = b.adjoint_backward(CH_BOX)
+            assert np.array_equal(a.populations(), before)
+            assert np.array_equal(b.populations(), before)
+            scale = np.abs(gb).max()
+            assert scale > 0
+            np.testing.assert_allclose(ga, gb, rtol=0, atol=1e-12 * scale)
+            ga2, _ = a.adjoint_backward(CH_BOX, dJ=2.0)  # repeatable with the kept records
+            np.testing.assert_allclose(ga2, 2.0 * ga, rtol=0, atol=1e-12 * scale)
+        assert a.steps_done == b.steps_done == 180
+
+
+def test_resident_records_out_of_memory_is_reported():
+    # records of 10^9 steps of the 20 x 10 x 8 channel (70 KB per step with the padded planes,
+    # 70 TB in all) do not fit: a refused allocation, LBM_ERR_OOM, and the handle stays usable
+    scn = _channel()
+    with build_domain(scn, "fp32") as d:
+        with pytest.raises(LbmError) as e:
+            d.adjoint_forward(10**9, 1)
+        assert e.value.code == capi.LBM_ERR_OOM
+        assert "step records" in str(e.value)
+        d.adjoint_forward(20, 1)
+        g, _ = d.adjoint_backward(CH_BOX)
+        assert np.all(np.isfinite(g))
+
+
 def test_backward_needs_the_forward_state():
     scn = _channel()
     with build_domain(scn) as d:
