@@ -460,6 +460,7 @@ void lbm_domain::finalize()
     if (wmask.n != nseg) wmask.alloc(nseg, "cudaMalloc(warp mask)");
     ops->warp_mask(dev, wmask.p, stream);
     dev.wmask = wmask.p;
+    dev.links = std::any_of(hmap.begin(), hmap.end(), [](uint8_t v) { return v >= kFirstHandler; }) ? 1 : 0;
     // merged inflow profile in reference cell order
     bool any_profile = false;
     for (const auto& p : profiles) any_profile = any_profile || !p.empty();

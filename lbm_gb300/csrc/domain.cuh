@@ -85,7 +85,6 @@ struct __align__(16) LinkRecord {
     float ir0;
     float c[kMaxRecordValues];
 };
-constexpr int kLinkWords = sizeof(LinkRecord) / 4;
 constexpr uint32_t kNoRecord = 0xffffffffu;
 static_assert(sizeof(LinkRecord) == 64, "LinkRecord is 16 words");
 
@@ -145,6 +144,8 @@ struct DomainDev {
     // One byte per row segment of the step kernel: bit w = the segment's warp w holds only
     // kFluidBulk cells (see warp_mask_kernel).
     const uint8_t* wmask;
+    // 1 when some cell is bound to a boundary handler (then fluid cells may have handler links)
+    int links;
     // Device error word: set to 1 by a kernel whose bounded wait gave up.
     int* err;
     // Step monitor accumulators: two sets of kMonBuckets x 4 doubles, used by alternate monitored

@@ -626,13 +626,6 @@ constexpr size_t edge_scratch_bytes()
 {
     return static_cast<size_t>(L::Q) * kRowCells * sizeof(typename Store<S>::C);
 }
-// (shifted storage) one LinkRecord per thread (64 bytes, 16-byte aligned: the destination of its
-// cp.async copies)
-template <class S>
-constexpr size_t link_smem_bytes()
-{
-    return Store<S>::kShifted ? static_cast<size_t>(kLinkWords) * kRowCells * 4 : 0;
-}
 // Warps with at most this many kFluidWall cells take the shared handler path (link_values_warp);
 // the others (a row along a wall, every lane with links) the per-lane one.
 #ifndef LBMG_WARP_LINK_CELLS
@@ -647,12 +640,29 @@ constexpr size_t warp_scratch_bytes()
 {
     return static_cast<size_t>(kRowCells / 32) * kWarpLinkCells * (L::Q + 4) * sizeof(typename Store<S>::C);
 }
-// Dynamic shared memory of a step-kernel block: a row block's stages, its LinkRecords and the warp
-// scratch, or an edge block's scratch from the start, whichever is larger.
+// The LinkRecords of the shared handler path's cells, copied into shared memory while the rows are
+// in flight: kWarpLinkCells per warp (shifted storage). Cells of warps with more linked cells (a
+// row along a wall) read theirs from global memory. One record per thread instead took the D3Q19
+// FP32 kernel's ten resident blocks past the 196 KB shared-memory carveout, and the smaller L1
+// left slowed the edge blocks' gathers by 7% on a periodic box.
+// Only FP32 stages them: the 16-bit kernels are issue-bound and ran 1.6% faster on the channel
+// reading their few records from global memory, while FP32, latency-bound, gained 1%.
+template <class S>
+constexpr bool stage_records()
+{
+    return Store<S>::kShifted && sizeof(S) == 4;
+}
+template <class S>
+constexpr size_t warp_records_bytes()
+{
+    return stage_records<S>() ? static_cast<size_t>(kRowCells / 32) * kWarpLinkCells * sizeof(LinkRecord) : 0;
+}
+// Dynamic shared memory of a step-kernel block: a row block's stages, the warp scratch and the
+// warp records, or an edge block's scratch from the start, whichever is larger.
 template <class L, class S>
 constexpr size_t row_smem_bytes()
 {
-    const size_t rows = segs<S>() * stage_bytes<L, S>() + link_smem_bytes<S>() + warp_scratch_bytes<L, S>();
+    const size_t rows = segs<S>() * stage_bytes<L, S>() + warp_scratch_bytes<L, S>() + warp_records_bytes<S>();
     const size_t edge = edge_scratch_bytes<L, S>();
     return rows > edge ? rows : edge;
 }
@@ -838,13 +848,15 @@ __device__ __forceinline__ void link_values(const StepParams<S>& P, int i, typen
 // typically the one cell next to an inlet or outlet at the end of a row, whose per-lane path would
 // hold the other 31 lanes for its whole length. Each such cell (a source lane, the k-th lane of
 // `need`) has put its post-collision populations and moments into slot k of the warp's scratch
-// (warp_link_source); here, per source, lane ip stores the value of link ip. Every lane of the warp
+// (warp_link_source), and its LinkRecord, if it has one (row), is slot k of recs where records are
+// staged (stage_records), else row `row` of ltab; here, per source, lane ip stores the value of
+// link ip. Every lane of the warp
 // calls it with the same `need` (at most kWarpLinkCells lanes with links); wl is 0 on the other
 // lanes. Same operations per value as link_values.
 template <class L, class S, bool ODD>
-__device__ __forceinline__ void link_values_warp(S* pop, unsigned need, int i, uint32_t wl, int has_rec,
-                                              const uint32_t* rec_warp, const typename Store<S>::C* scr,
-                                              size_t ps, int sy, int sz)
+__device__ __forceinline__ void link_values_warp(S* pop, unsigned need, int i, uint32_t wl, uint32_t row,
+                                              const LinkRecord* recs, const LinkRecord* ltab,
+                                              const typename Store<S>::C* scr, size_t ps, int sy, int sz)
 {
     using St = Store<S>;
     using T = typename St::C;
@@ -852,11 +864,11 @@ __device__ __forceinline__ void link_values_warp(S* pop, unsigned need, int i, u
     constexpr int SW = Q + 4;  // scratch words of one source
     constexpr unsigned kFull = 0xffffffffu;
     const int ip = static_cast<int>(threadIdx.x & 31u);  // this lane's link
-    for (unsigned rem = need; rem; rem &= rem - 1u, scr += SW) {
+    for (unsigned rem = need; rem; rem &= rem - 1u, scr += SW, ++recs) {
         const int src = __ffs(rem) - 1;
         const uint32_t swl = __shfl_sync(kFull, wl, src);
         const int si = __shfl_sync(kFull, i, src);
-        const int srec = __shfl_sync(kFull, has_rec, src);
+        const uint32_t srow = __shfl_sync(kFull, row, src);  // the source's LinkRecord row
         if (ip < Q && ((swl >> ip) & 1u)) {
             // direction p = inv(ip): after an odd step slot ip at the source cell x, after an even
             // step plane p at x + c_p
@@ -864,8 +876,8 @@ __device__ __forceinline__ void link_values_warp(S* pop, unsigned need, int i, u
             const int cx = rt_c<L>(p, 0), cy = rt_c<L>(p, 1), cz = rt_c<L>(p, 2);
             T v = scr[p];
             if constexpr (St::kShifted) {
-                const uint32_t* r = rec_warp + kLinkWords * src;
-                if (srec && ((r[0] >> ip) & 1u)) {
+                const uint32_t* r = reinterpret_cast<const uint32_t*>(stage_records<S>() ? recs : ltab + srow);
+                if (srow != kNoRecord && ((r[0] >> ip) & 1u)) {
                     const uint32_t wallm = r[1], valm = wallm | r[2];
                     if ((valm >> ip) & 1u) {
                         const int k = min(__popc(valm & ((1u << ip) - 1u)), kMaxRecordValues - 1);
@@ -945,7 +957,10 @@ __device__ __forceinline__ V opaque(V v)
     return v;
 }
 
-template <class L, class S, bool ODD, bool INSTR>
+// LINKS: the handler path is compiled in (domains with handler cells). Without it a kFluidWall cell
+// would lose its handler values, so a domain without handler cells, which has none, is the only
+// user of LINKS = false (see the step launcher).
+template <class L, class S, bool ODD, bool INSTR, bool LINKS>
 __device__ __forceinline__ void row_block(const StepParams<S>& P, int rb, int nseg, const FastDiv& dx, const FastDiv& dy,
                                           unsigned char* smem_raw, uint64_t* bars, typename Store<S>::C (&macc)[4],
                                           int& ncell)
@@ -1005,24 +1020,38 @@ __device__ __forceinline__ void row_block(const StepParams<S>& P, int rb, int ns
         // are all kFluidBulk (the segment's warp mask) loads neither.
         bool bulk = true;
         uint2 lk = make_uint2(0u, kNoRecord);
-        if (!((P.wmask[seg0 + s] >> (tx >> 5)) & 1u)) {
+        LinkRecord* recs = reinterpret_cast<LinkRecord*>(smem_raw + kSegs * SB + warp_scratch_bytes<L, S>()) +
+                           (tx >> 5) * kWarpLinkCells;
+        bool staged = false;
+        if (!((P.wmask[seg0 + s] >> (tx >> 5)) & 1u)) {  // (warp-uniform)
             const bool face = x == 1 || x == P.g.xl || y == 1 || y == P.g.yl || z == 1 || z == P.g.zl;
             const uint2 lkf = face && x <= P.g.xl ? P.link[i] : make_uint2(0u, kNoRecord);
             const uint8_t fl = x <= P.g.xl ? P.flag[i] : static_cast<uint8_t>(kFluidEdge);
             bulk = fl == kFluidBulk || fl == kFluidWall;
             lk = fl != kFluidWall ? make_uint2(0u, kNoRecord) : face ? lkf : P.link[i];
-        }
-        const uint32_t wl = lk.x;
-        uint32_t* rec = nullptr;
-        if constexpr (St::kShifted) {
-            if (lk.y != kNoRecord) {
-                rec = reinterpret_cast<uint32_t*>(smem_raw + kSegs * SB) + kLinkWords * tx;
-                const char* src = reinterpret_cast<const char*>(P.ltab + lk.y);
+            // the cell's LinkRecord (shifted storage): in a warp with few linked cells copied into
+            // the warp's record slot (the cell's rank among them) while the rows are in flight, else
+            // read from global memory where it is used (fetched into L1 now)
+            if constexpr (St::kShifted && LINKS) {
+                const unsigned need_e = stage_records<S>() ? __ballot_sync(0xffffffffu, lk.x != 0u) : ~0u;
+                if (lk.y != kNoRecord) {
+                    const char* src = reinterpret_cast<const char*>(P.ltab + lk.y);
+                    if (stage_records<S>() && __popc(need_e) <= kWarpLinkCells) {
+                        char* dst = reinterpret_cast<char*>(recs + __popc(need_e & ((1u << (tx & 31)) - 1u)));
 #pragma unroll
-                for (int w = 0; w < kLinkWords / 4; ++w) cp_async16(rec + 4 * w, src + 16 * w);
-                cp_async_commit();
+                        for (int w = 0; w < static_cast<int>(sizeof(LinkRecord) / 16); ++w)
+                            cp_async16(dst + 16 * w, src + 16 * w);
+                        cp_async_commit();
+                        staged = true;
+                    } else {
+                        prefetch_l1(src);
+                    }
+                }
             }
         }
+        const uint32_t wl = lk.x;
+        const uint32_t* rec = St::kShifted && lk.y != kNoRecord
+                                  ? reinterpret_cast<const uint32_t*>(P.ltab + lk.y) : nullptr;
         if (!mbar_wait_bounded(&bars[s], 0, kRowWaitPolls)) {
             // the step's results are invalid; still never leave while copies may land here (this
             // drain wait is bounded too: if it also gives up the block returns regardless)
@@ -1045,35 +1074,27 @@ __device__ __forceinline__ void row_block(const StepParams<S>& P, int rb, int ns
                 store_cell<L, S, ODD, true>(pop + i, f, PS, sy, sz);
             else
                 store_cell<L, S, ODD, false>(pop + i, f, PS, sy, sz);
-        } else if constexpr (St::kShifted) {
-            if (rec) cp_async_wait_all();  // no copy may still be landing when the block ends
         }
         // handler values, into slots that no cell's own stores touch: shared by the warp when
         // few of its cells have links, else per lane
-        const uint32_t wlb = bulk ? wl : 0u;
-        const unsigned need = __ballot_sync(0xffffffffu, wlb != 0u);
-        if (need) {
+        const uint32_t wlb = LINKS && bulk ? wl : 0u;
+        const unsigned need = LINKS ? __ballot_sync(0xffffffffu, wlb != 0u) : 0u;
+        if (LINKS && need) {
+            // (need equals need_e unless the row wait gave up, which leaves need empty)
             if (__popc(need) <= kWarpLinkCells) {
-                const uint32_t* rec_warp =
-                    reinterpret_cast<const uint32_t*>(smem_raw + kSegs * SB) + kLinkWords * (tx & ~31);
-                T* scr = reinterpret_cast<T*>(smem_raw + kSegs * SB + link_smem_bytes<S>()) +
-                         (tx >> 5) * kWarpLinkCells * (Q + 4);
+                T* scr = reinterpret_cast<T*>(smem_raw + kSegs * SB) + (tx >> 5) * kWarpLinkCells * (Q + 4);
                 if (wlb) {
-                    if constexpr (St::kShifted) {
-                        if (rec) cp_async_wait_all();  // this lane's LinkRecord has landed
-                    }
+                    if (staged) cp_async_wait_all();  // this lane's record has landed
                     warp_link_source<L, S>(need, f, m, scr);
                 }
                 __syncwarp();
-                link_values_warp<L, S, ODD>(pop, need, i, wlb, rec != nullptr, rec_warp, scr, PS, sy, sz);
-                __syncwarp();  // the scratch is read before the warp's next segment writes it
+                link_values_warp<L, S, ODD>(pop, need, i, wlb, lk.y, recs, P.ltab, scr, PS, sy, sz);
+                __syncwarp();  // scratch and records are read before the warp's next segment writes them
             } else if (wlb) {
-                if constexpr (St::kShifted) {
-                    if (rec) cp_async_wait_all();
-                }
                 link_values<L, S, ODD>(P, i, f, m, wlb, rec, opaque(PS), opaque(sy));
             }
         }
+        if (staged) cp_async_wait_all();  // no copy may still be landing when the block ends
         if constexpr (INSTR) {
 #pragma unroll
             for (int k = 0; k < 4; ++k) macc[k] += m[k];
@@ -1130,7 +1151,7 @@ constexpr int min_blocks()
 constexpr double kEdgeSpan = LBMG_EDGE_SPAN;
 // INSTR: the step monitor and the adjoint's record may be active (P.mon / P.rec are tested);
 // plain steps are compiled without them.
-template <class L, class S, bool ODD, bool INSTR>
+template <class L, class S, bool ODD, bool INSTR, bool LINKS>
 __global__ void __launch_bounds__(kRowCells, min_blocks<L, S, ODD, INSTR>())
     step_kernel(const StepParams<S> P, int n_edge_blocks, FastDiv edge_stride, int nseg, FastDiv nseg_x, FastDiv yl)
 {
@@ -1152,9 +1173,9 @@ __global__ void __launch_bounds__(kRowCells, min_blocks<L, S, ODD, INSTR>())
     if (b < interleaved && b == e * static_cast<int>(edge_stride.d))
         edge_block<L, S, ODD, INSTR>(P, e, smem_raw, macc, ncell);
     else if (b < interleaved)
-        row_block<L, S, ODD, INSTR>(P, b - (e + 1), nseg, nseg_x, yl, smem_raw, bars, macc, ncell);
+        row_block<L, S, ODD, INSTR, LINKS>(P, b - (e + 1), nseg, nseg_x, yl, smem_raw, bars, macc, ncell);
     else
-        row_block<L, S, ODD, INSTR>(P, b - n_edge_blocks, nseg, nseg_x, yl, smem_raw, bars, macc, ncell);
+        row_block<L, S, ODD, INSTR, LINKS>(P, b - n_edge_blocks, nseg, nseg_x, yl, smem_raw, bars, macc, ncell);
     if constexpr (INSTR) {
         if (P.mon) monitor_block_add<S>(P.mon, macc, ncell);
     }

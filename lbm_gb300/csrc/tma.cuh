@@ -90,6 +90,9 @@ __device__ __forceinline__ void cp_async16(void* smem_dst, const void* gmem_src)
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
+// A hint: the L1 line at p is fetched now, for a read that follows later.
+__device__ __forceinline__ void prefetch_l1(const void* p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
+
 // Programmatic dependent launch (griddepcontrol). grid_dep_wait blocks until the kernel this grid
 // follows in its stream has completed and its writes are visible; it returns at once for a launch
 // without the programmatic attribute. grid_dep_launch lets the next kernel in the stream, if it was
