@@ -1107,9 +1107,9 @@ __device__ __forceinline__ void row_block(const StepParams<S>& P, int rb, int ns
 // bound; ptxas then picks fewer registers than with an explicit 1). Shifted D3Q19 kernels: 10
 // blocks (48 registers; unbounded they take 56, 9 blocks). D3Q15: 12 blocks (40 registers) for
 // FP32 (46.5k against 45.4k MLUPS at 10 on the 256x128x128 channel), 10 for 16-bit storage (67.3k
-// against 65.3k at 12, where the 40-register kernels spill). D3Q27: unbounded for FP32 (72-80
-// registers; 23.7k against 23.5k at 8) and 8 blocks for 16-bit storage (64 registers; 40.3k
-// against 38.7k unbounded). FP64 is never bounded. LBMG_MINB_Q15 / LBMG_MINB_Q27 set the D3Q15
+// against 65.3k at 12, where the 40-register kernels spill). D3Q27: 7 blocks for FP32 (72
+// registers; 24.2k against 23.9k unbounded at 72-80 and 23.9k at 8) and 8 blocks for 16-bit
+// storage (64 registers; 40.3k against 38.7k unbounded). FP64 is never bounded. LBMG_MINB_Q15 / LBMG_MINB_Q27 set the D3Q15
 // and D3Q27 values of every storage type, LBMG_MINB_EVEN / LBMG_MINB_ODD the shifted-storage
 // values, in tuning builds.
 template <class L, class S, bool ODD, bool INSTR>
@@ -1137,7 +1137,7 @@ constexpr int min_blocks()
         if (L::Q == 27) return LBMG_MINB_Q27;
 #endif
         if (L::Q == 15) return k16 ? 10 : 12;
-        return k16 ? 8 : 0;
+        return k16 ? 8 : 7;
     }
 }
 
