@@ -116,3 +116,43 @@ def test_headline_channel_full_size_reduced_precision(headline_port, precision):
     assert eu <= tol["u_rel_l2"], (eu, e)
     assert e["handler_entries"] <= tol["entries"], e
     assert max(e["u_linked"], e["rho_linked"]) <= tol["moments"], e
+
+
+# ------------------------------------------------------------------------------------------
+# The warp-shared handler path with LinkRecords: a moving wall on the x0 face (velocity in y and
+# z) leaves one linked cell, x = 1, in the first warp of every inner row, so each of those warps
+# hands that cell's moving-wall values (record constants times the cell's density) to the warp
+# (FP32 with the record staged in shared memory, 16-bit storage reading it from global memory);
+# the wall rows, every lane linked, take the per-lane path. 120 steps against the C port of the
+# reference, per-cell maxima as in the headline test.
+# ------------------------------------------------------------------------------------------
+XLID_STEPS = 120
+TOL_XLID = {  # the golden cases' bounds (entries for FP32 as the headline's)
+    "fp32": {"entries": 5e-8, "moments": 1e-6},
+    "fp16": {"entries": 1e-4, "moments": 2e-4},
+    "bf16": {"entries": 1e-3, "moments": 2e-3},
+}
+
+
+def xlid_scenario(q):
+    s = S.Scenario("XLid", q, 96, 32, 24, 0.6)
+    for f in ("y0", "ymax", "z0", "zmax", "xmax"):
+        s.add_face(f, "noslip")
+    s.add_face("x0", "movingwall", (0.0, 0.05, -0.02))
+    return s
+
+
+@pytest.mark.parametrize("q", [19, 27])
+def test_moving_wall_values_through_the_warp_shared_path(q):
+    scn = xlid_scenario(q)
+    want = oracle.run_port(scn, XLID_STEPS)
+    for precision, tol in TOL_XLID.items():
+        with build_domain(scn, precision) as dom:
+            dom.step(XLID_STEPS)
+            pops = dom.populations()
+            rho, u = dom.moments()
+        e = precision_errors(scn, pops, rho, u, want["pops"], want["rho"], want["u"])
+        print(f"x-lid D3Q{q} {precision}: {e}")
+        assert e["handler_entries"] <= tol["entries"], (precision, e)
+        assert e["fluid_entries"] <= tol["entries"], (precision, e)
+        assert max(e["u_linked"], e["rho_linked"], e["u_bulk"], e["rho_bulk"]) <= tol["moments"], (precision, e)
