@@ -185,8 +185,9 @@ int lbm_adjoint_objective_ke(lbm_domain* d, const int64_t box[6], double* J);
  * state is left as lbm_adjoint_forward left it, so the call may be repeated (another box or dJ).
  * Device memory (allocated by the first call and kept with the handle for the next ones, until a
  * geometry change, a run with another checkpoint interval, or lbm_destroy): two adjoint population
- * stores (Q values per cell in the compute type: FP32, or FP64 for FP64 storage), ckpt_every * 4
- * recorded values per cell, one copy of the population store and 3 doubles per cell (after a
+ * stores (Q values per cell in the compute type: FP32, or FP64 for FP64 storage), 2 * ckpt_every * 4
+ * recorded values per cell (the recompute of one checkpoint segment overlaps the adjoint steps of
+ * the next), one copy of the population store and 3 doubles per cell (after a
  * ckpt_every = 1 forward: the adjoint stores and the gradients only, beside its records). The
  * gradients are scaled by dJ on the device and copied into the caller's arrays. Synchronises. */
 int lbm_adjoint_backward(lbm_domain* d, const int64_t box[6], double dJ, double* grad_inflow,

@@ -132,11 +132,26 @@ struct AdjointRun {
     DevBuf<unsigned char> mu[2];   // adjoint populations mu_t, mu_{t-1}
     DevBuf<unsigned char> rec;     // the recorded mass and momentum of a segment's k steps (of
                                    // all n steps when resident)
+    DevBuf<unsigned char> rec2;    // a second segment record: the recompute of one segment
+                                   // overlaps the adjoint steps of the next
     DevBuf<unsigned char> backup;  // the state the forward run left
     DevBuf<double> gin, gwall;     // gradients (inflow cells, wall handlers)
+    // the recompute stream and its events (record buffer b filled / read), created on first use
+    cudaStream_t rstream = nullptr;
+    cudaEvent_t filled[2] = {nullptr, nullptr};
+    cudaEvent_t drained[2] = {nullptr, nullptr};
     void release_workspace()
     {
-        mu[0].release(); mu[1].release(); rec.release(); backup.release(); gin.release(); gwall.release();
+        mu[0].release(); mu[1].release(); rec.release(); rec2.release(); backup.release(); gin.release();
+        gwall.release();
+    }
+    ~AdjointRun()
+    {
+        for (int b = 0; b < 2; ++b) {
+            if (filled[b]) cudaEventDestroy(filled[b]);
+            if (drained[b]) cudaEventDestroy(drained[b]);
+        }
+        if (rstream) cudaStreamDestroy(rstream);
     }
 };
 
@@ -1037,7 +1052,7 @@ int lbm_memory_info(const lbm_domain* d, uint64_t* device_bytes, uint64_t* step_
             *device_bytes = m->pop.bytes() + m->flag.bytes() + m->bc.bytes() + m->profile.bytes() + m->gf_xyz.bytes() +
                             m->gf_pop.bytes() + m->fs_link.bytes() + m->red.bytes() + m->link.bytes() + m->edge.bytes() +
                             m->errword.bytes() + m->mon.bytes() + m->mon_ring.bytes() + m->stage.bytes() + m->ltab.bytes() +
-                            m->wmask.bytes() + m->adj.mu[0].bytes() + m->adj.mu[1].bytes() + m->adj.rec.bytes() + m->adj.backup.bytes() +
+                            m->wmask.bytes() + m->adj.mu[0].bytes() + m->adj.mu[1].bytes() + m->adj.rec.bytes() + m->adj.rec2.bytes() + m->adj.backup.bytes() +
                             m->adj.gin.bytes() + m->adj.gwall.bytes();
         if (device_bytes)
             for (const auto& c : m->adj.ckpt) *device_bytes += c->bytes();
@@ -1150,12 +1165,21 @@ int lbm_adjoint_backward(lbm_domain* d, const int64_t box[6], double dJ, double*
             gin.alloc(3 * d->ng, "cudaMalloc(inflow gradient)");
             gwall.alloc(3 * kMaxHandlers, "cudaMalloc(wall gradient)");
         }
+        const long long nseg = a.resident ? 1 : static_cast<long long>(a.ckpt.size());
         if (a.resident) {
             backup.release();  // no recompute: the state is never touched
         } else {
-            if (rec.bytes() != static_cast<size_t>(a.k) * rec_bytes)
-                rec.alloc(static_cast<size_t>(a.k) * rec_bytes, "cudaMalloc(recompute record)");
+            const size_t seg_rec = static_cast<size_t>(a.k) * rec_bytes;
+            if (rec.bytes() != seg_rec) rec.alloc(seg_rec, "cudaMalloc(recompute record)");
+            if (nseg > 1 && a.rec2.bytes() != seg_rec) a.rec2.alloc(seg_rec, "cudaMalloc(recompute record)");
             if (backup.bytes() != d->pop.bytes()) backup.alloc(d->pop.bytes(), "cudaMalloc(state backup)");
+            if (!a.rstream) {
+                check(cudaStreamCreateWithFlags(&a.rstream, cudaStreamNonBlocking), "cudaStreamCreate(recompute)");
+                for (int k = 0; k < 2; ++k) {
+                    check(cudaEventCreateWithFlags(&a.filled[k], cudaEventDisableTiming), "cudaEventCreate");
+                    check(cudaEventCreateWithFlags(&a.drained[k], cudaEventDisableTiming), "cudaEventCreate");
+                }
+            }
         }
         check(cudaMemsetAsync(gin.p, 0, gin.bytes(), d->stream), "clear gradient");
         check(cudaMemsetAsync(gwall.p, 0, gwall.bytes(), d->stream), "clear gradient");
@@ -1165,32 +1189,53 @@ int lbm_adjoint_backward(lbm_domain* d, const int64_t box[6], double dJ, double*
             check(cudaMemcpyAsync(backup.p, d->pop.p, d->pop.bytes(), cudaMemcpyDeviceToDevice, d->stream),
                   "state backup");
 
-        // resident: one segment of all n steps whose records the forward wrote
-        const long long nseg = a.resident ? 1 : static_cast<long long>(a.ckpt.size());
+        // resident: one segment of all n steps whose records the forward wrote. Otherwise segment
+        // j is recomputed from its checkpoint on the recompute stream into record buffer j % 2
+        // while the handle's stream runs the adjoint steps of segment j + 1 from the other buffer:
+        // both kernels are latency-bound on small domains and fill the GPU together. The adjoint
+        // steps touch no population; the recompute waits until its buffer has been read.
         const long long seg_len = a.resident ? a.n : a.k;
+        unsigned char* const recs[2] = {rec.p, a.rec2.p};
+        auto recompute = [&](long long j) {
+            const int bj = static_cast<int>(j & 1);
+            const long long c = a.s0 + j * seg_len;
+            const long long len = std::min<long long>(seg_len, a.n - j * seg_len);
+            check(cudaStreamWaitEvent(a.rstream, a.drained[bj], 0), "recompute wait");
+            check(cudaMemcpyAsync(d->pop.p, a.ckpt[j]->p, d->pop.bytes(), cudaMemcpyDeviceToDevice, a.rstream),
+                  "restore checkpoint");
+            for (long long r = 1; r <= len; ++r)  // recording rec_{c+r}
+                d->ops->step(d->dev, c + r, -1, nullptr, recs[bj] + (r - 1) * rec_bytes, a.rstream);
+            check(cudaEventRecord(a.filled[bj], a.rstream), "recompute done");
+        };
+        if (!a.resident) {
+            // both buffers free, after the clears and the state backup above
+            for (int k = 0; k < 2; ++k) check(cudaEventRecord(a.drained[k], d->stream), "adjoint start");
+            recompute(nseg - 1);
+        }
         int cur = 0;
         long long t_cur = 0;  // mu[cur] holds mu_{t_cur}
         for (long long j = nseg - 1; j >= 0; --j) {
+            const int bj = static_cast<int>(j & 1);
             const long long c = a.s0 + j * seg_len;
             const long long len = std::min<long long>(seg_len, a.n - j * seg_len);
+            const unsigned char* rj = a.resident ? rec.p : recs[bj];
             if (!a.resident) {
-                check(cudaMemcpyAsync(d->pop.p, a.ckpt[j]->p, d->pop.bytes(), cudaMemcpyDeviceToDevice, d->stream),
-                      "restore checkpoint");
-                for (long long r = 1; r <= len; ++r)  // recompute, recording rec_{c+r}
-                    d->ops->step(d->dev, c + r, -1, nullptr, rec.p + (r - 1) * rec_bytes, d->stream);
+                if (j > 0) recompute(j - 1);  // runs alongside this segment's adjoint steps
+                check(cudaStreamWaitEvent(d->stream, a.filled[bj], 0), "adjoint wait");
             }
             if (j == nseg - 1) {
-                d->ops->adj_terminal(d->dev, rec.p + (len - 1) * rec_bytes, mu[cur].p, b, d->stream);
+                d->ops->adj_terminal(d->dev, rj + (len - 1) * rec_bytes, mu[cur].p, b, d->stream);
                 t_cur = c + len;
             }
             // mu_t -> mu_{t-1} with the record of step t-1; the run's first step (t = s0 + 1) pulls
             // the boundary values the starting state holds, so the loop ends at t = s0 + 2
             for (long long t = t_cur; t >= c + 2; --t) {
-                d->ops->adj_step(d->dev, mu[cur].p, mu[1 - cur].p, rec.p + (t - c - 2) * rec_bytes, 1, 1, gin.p,
+                d->ops->adj_step(d->dev, mu[cur].p, mu[1 - cur].p, rj + (t - c - 2) * rec_bytes, 1, 1, gin.p,
                                  gwall.p, d->stream);
                 cur = 1 - cur;
                 t_cur = t - 1;
             }
+            if (!a.resident) check(cudaEventRecord(a.drained[bj], d->stream), "adjoint segment done");
         }
         if (!a.resident)
             check(cudaMemcpyAsync(d->pop.p, backup.p, d->pop.bytes(), cudaMemcpyDeviceToDevice, d->stream),
