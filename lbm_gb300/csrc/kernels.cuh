@@ -569,11 +569,13 @@ __device__ __forceinline__ void store_edge_populations(const StepParams<S>& P, i
 //   completing on its own mbarrier. Each copied row is the segment widened by 16 bytes on both
 //   sides, which keeps source and size 16-byte aligned and covers the +-1 shift in x of the
 //   odd-step pulls. The loads in flight are bounded by shared memory rather than registers.
-// - While the rows land, each thread loads its flag and link entry and, for a cell with a
-//   LinkRecord, copies the record into shared memory.
-// - Each cell then collides from the stage, writes the handler values of its links
-//   (link_values) and stores its Q populations (store_cell). Handler values sit where the next
-//   step pulls them, so no cell needs a special load.
+// - While the rows land, each thread loads its flag and link entry (warps of bulk cells only, marked
+//   by the segment's warp mask, load neither); FP32 copies the LinkRecords of warps with few linked
+//   cells into shared memory.
+// - Each cell then collides from the stage and stores its Q populations (store_cell), and the
+//   handler values of its links are stored (link_values per lane, or link_values_warp shared by
+//   a warp with few linked cells). Handler values sit where the next step pulls them, so no cell
+//   needs a special load.
 //
 // Edge blocks take the cells a row block cannot: a periodic wrap, a free-slip or ghost-fluid
 // neighbour, or more handler constants than a record holds. They work from the sorted list
