@@ -1099,6 +1099,7 @@ int lbm_adjoint_forward(lbm_domain* d, int64_t nsteps, int64_t ckpt_every)
         if (a.resident) {
             // every step records its cell moments (what the backward's recompute would record)
             a.backup.release();
+            a.rec2.release();
             if (!a.rec.p) a.rec.alloc(rec_need, "cudaMalloc(step records)");
             for (long long r = 0; r < nsteps; ++r)
                 d->ops->step(d->dev, d->steps + 1 + r, -1, nullptr, a.rec.p + r * rec_bytes, d->stream);
