@@ -852,9 +852,8 @@ __device__ __forceinline__ void link_values(const StepParams<S>& P, int i, typen
 // `need`) has put its post-collision populations and moments into slot k of the warp's scratch
 // (warp_link_source), and its LinkRecord, if it has one (row), is slot k of recs where records are
 // staged (stage_records), else row `row` of ltab; here, per source, lane ip stores the value of
-// link ip. Every lane of the warp
-// calls it with the same `need` (at most kWarpLinkCells lanes with links); wl is 0 on the other
-// lanes. Same operations per value as link_values.
+// link ip. Every lane of the warp calls it with the same `need` (at most kWarpLinkCells lanes with
+// links); wl is 0 on the other lanes. Same operations per value as link_values.
 template <class L, class S, bool ODD>
 __device__ __forceinline__ void link_values_warp(S* pop, unsigned need, int i, uint32_t wl, uint32_t row,
                                               const LinkRecord* recs, const LinkRecord* ltab,
