@@ -224,7 +224,11 @@ def test_backward_restores_state_and_can_repeat():
         g1, _ = d.adjoint_backward(CH_BOX)
         assert np.array_equal(d.populations(), before)
         g2, _ = d.adjoint_backward(CH_BOX, dJ=2.0)
-        assert np.array_equal(2.0 * g1, g2)
+        # the gradients are sums of FP64 atomic adds (several cells and steps per inflow cell), whose
+        # order follows the block scheduling, which the recompute stream running beside the adjoint
+        # steps changes from call to call: equal to rounding, not bit for bit
+        np.testing.assert_allclose(g2, 2.0 * g1, rtol=1e-12, atol=1e-15 * np.abs(g1).max())
+        assert np.abs(g1).max() > 0
         assert d.steps_done == 30
 
 
@@ -311,9 +315,10 @@ def test_torch_autograd_function_wrapper():
     prof = torch.tensor(_channel().boundaries[0].profile, requires_grad=True)
     J = KineticEnergy.apply(prof, 60, 16, CH_BOX)
     (g,) = torch.autograd.grad(3.0 * J, prof)
-    # the same gradient as the C ABI call, scaled by the upstream factor
+    # the same gradient as the C ABI call, scaled by the upstream factor (to rounding: the FP64
+    # atomic adds of the gradient sums run in scheduling order)
     _, gin, _ = _adjoint(_channel(), 60, 16, CH_BOX)
-    assert np.array_equal(g.numpy(), 3.0 * gin)
+    np.testing.assert_allclose(g.numpy(), 3.0 * gin, rtol=1e-12, atol=1e-15 * np.abs(gin).max())
     # and a directional finite difference through the wrapper itself
     v = torch.zeros_like(prof)
     k = _inflow_index(_channel(), 5, 4)
